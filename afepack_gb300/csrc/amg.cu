@@ -1,0 +1,707 @@
+// AMG hierarchy, V-cycle and preconditioned CG (AMGSolver::reinit / solve,
+// src/AMGSolver.cpp:384-639, and the CG of
+// examples/FAST/src/poisson_solver_comparison_afepack.cpp:197-253).
+//
+// Setup reproduces the reference hierarchy: per level the host runs the C/F
+// splitting (host_project) on the level matrix, the GPU forms P A P^T
+// (galerkin_product), and the coarse matrix comes back to the host for the
+// next splitting, until the reference's stop rule holds -- or, GB300-side,
+// until a level is small enough (opts.dense_tail) to be solved through a
+// dense inverse, the reference's own coarsest-level treatment.
+//
+// For the solve every smoothed level is colour-permuted: rows are grouped by
+// greedy colour class so that a Gauss-Seidel class is a contiguous row
+// range.  P and P^T are stored explicitly in the permuted numbering, so
+// restriction and prolongation are gathers without atomics.  The V-cycle is
+// captured once into a CUDA graph and replayed.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "kernels.cuh"
+#include "solve.cuh"
+
+namespace afp {
+
+struct Level {
+  int64_t n = 0, nnz = 0;
+  DevBuf<int> rp, ci;
+  DevBuf<double> va;
+  DevBuf<float> va32;
+  int vec = 8;
+  std::vector<int64_t> cls;  // class boundaries (cls.size()-1 classes)
+  bool overflow = false;     // the last class is the l1-Jacobi overflow class
+  DevBuf<double> l1d;
+  DevBuf<float> l1d32;
+  // restriction P (n_{l+1} x n_l) and prolongation P^T (n_l x n_{l+1})
+  DevBuf<int> prp, pci, trp, tci;
+  DevBuf<double> pva, tva;
+  DevBuf<__nv_bfloat16> pva16, tva16;
+  int64_t pnnz = 0;
+  int pvec = 8, tvec = 8;
+  DevBuf<int> perm;  // solve order -> reference order
+  DevBuf<double> x, r, tmp;
+  DevBuf<float> x32, r32, tmp32;
+
+  template <class X>
+  CSRView<X> A() const;
+};
+
+template <>
+CSRView<double> Level::A<double>() const {
+  return {n, rp.get(), ci.get(), va.get(), vec};
+}
+template <>
+CSRView<float> Level::A<float>() const {
+  return {n, rp.get(), ci.get(), va32.get(), vec};
+}
+
+}  // namespace afp
+
+using namespace afp;
+
+struct afp_amg {
+  afp_context* ctx = nullptr;
+  afp_amg_opts opts{};
+  int n_project = 0;   // levels built (projections)
+  bool most_full = true;
+  int t = 0;           // smoothed levels 0..t-1, level t is the tail
+  bool tail_dense = true;
+  std::vector<Level> lv;
+  std::vector<HostCSR> refA, refP;  // reference-order copies for download
+  DevBuf<double> tail_inv;
+  DevBuf<float> tail_inv32;
+  // solver vectors (level-0 solve order)
+  DevBuf<double> b, x, r, z, p, q, tmp;
+  DevBuf<float> r32, z32;
+  cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
+  int64_t graph64_nodes = 0, graph32_nodes = 0;
+
+  ~afp_amg() {
+    if (graph64) cudaGraphExecDestroy(graph64);
+    if (graph32) cudaGraphExecDestroy(graph32);
+  }
+};
+
+namespace afp {
+namespace {
+
+struct DevCSR {
+  int64_t m = 0, n = 0, nnz = 0;
+  DevBuf<int> rp, ci;
+  DevBuf<double> va;
+};
+
+void upload_host_csr(const afp_context* ctx, const HostCSR& H, DevCSR& D) {
+  D.m = H.m;
+  D.n = H.n;
+  D.nnz = H.nnz();
+  D.rp.alloc(ctx, H.m + 1);
+  D.ci.alloc(ctx, D.nnz);
+  D.va.alloc(ctx, D.nnz);
+  D.rp.upload(H.rowptr.data(), H.m + 1);
+  D.ci.upload(H.cols.data(), D.nnz);
+  D.va.upload(H.vals.data(), D.nnz);
+}
+
+void download_host_csr(const afp_context* ctx, int64_t m, int64_t n, int64_t nnz, const int* rp, const int* ci,
+                       const double* va, HostCSR& H) {
+  H.m = m;
+  H.n = n;
+  H.rowptr.resize(m + 1);
+  H.cols.resize(nnz);
+  H.vals.resize(nnz);
+  copy(ctx, H.rowptr.data(), rp, sizeof(int) * (m + 1));
+  copy(ctx, H.cols.data(), ci, sizeof(int) * nnz);
+  copy(ctx, H.vals.data(), va, sizeof(double) * nnz);
+  sync(ctx);
+}
+
+template <class X>
+X* lvx(afp_amg* h, int l);
+template <>
+double* lvx<double>(afp_amg* h, int l) {
+  return h->lv[l].x.get();
+}
+template <>
+float* lvx<float>(afp_amg* h, int l) {
+  return h->lv[l].x32.get();
+}
+template <class X>
+X* lvr(afp_amg* h, int l);
+template <>
+double* lvr<double>(afp_amg* h, int l) {
+  return h->lv[l].r.get();
+}
+template <>
+float* lvr<float>(afp_amg* h, int l) {
+  return h->lv[l].r32.get();
+}
+template <class X>
+X* lvt(afp_amg* h, int l);
+template <>
+double* lvt<double>(afp_amg* h, int l) {
+  return h->lv[l].tmp.get();
+}
+template <>
+float* lvt<float>(afp_amg* h, int l) {
+  return h->lv[l].tmp32.get();
+}
+template <class X>
+const X* l1(const Level& L);
+template <>
+const double* l1<double>(const Level& L) {
+  return L.l1d.get();
+}
+template <>
+const float* l1<float>(const Level& L) {
+  return L.l1d32.get();
+}
+
+template <class X>
+void smooth(afp_amg* h, int l, X* x, const X* r, bool backward) {
+  const Level& L = h->lv[l];
+  CSRView<X> A = L.A<X>();
+  const int K = (int)L.cls.size() - 1;
+  for (int s = 0; s < h->opts.smooth_step; ++s) {
+    for (int q = 0; q < K; ++q) {
+      const int c = backward ? K - 1 - q : q;
+      const int64_t r0 = L.cls[c], r1 = L.cls[c + 1];
+      if (L.overflow && c == K - 1)
+        jacobi_l1_class<X>(h->ctx, A, r0, r1, x, r, l1<X>(L), lvt<X>(h, l));
+      else
+        gs_class<X>(h->ctx, A, r0, r1, x, r);
+    }
+  }
+}
+
+// One V-cycle on x0 (level-0 solve order) for right-hand side r0.
+template <class X, class PV>
+void vcycle(afp_amg* h, X* x0, const X* r0, bool zero_init) {
+  const afp_context* ctx = h->ctx;
+  const int t = h->t;
+  for (int l = 0; l < t; ++l) {
+    Level& L = h->lv[l];
+    X* x = l == 0 ? x0 : lvx<X>(h, l);
+    const X* r = l == 0 ? r0 : lvr<X>(h, l);
+    if (l > 0 || zero_init) fill_zero<X>(ctx, L.n, x);
+    smooth<X>(h, l, x, r, false);
+    residual<X>(ctx, L.A<X>(), x, r, lvt<X>(h, l));
+    CSRView<PV> P{h->lv[l + 1].n, L.prp.get(), L.pci.get(), nullptr, L.pvec};
+    if constexpr (std::is_same<PV, double>::value) P.vals = L.pva.get();
+    else P.vals = L.pva16.get();
+    spmv<PV, X>(ctx, P, lvt<X>(h, l), lvr<X>(h, l + 1), false);
+  }
+  X* xt = t == 0 ? x0 : lvx<X>(h, t);
+  const X* rt = t == 0 ? r0 : lvr<X>(h, t);
+  if (h->tail_dense) {
+    const X* inv;
+    if constexpr (std::is_same<X, double>::value) inv = h->tail_inv.get();
+    else inv = h->tail_inv32.get();
+    dense_gemv<X>(ctx, h->lv[t].n, inv, rt, xt);
+  } else {
+    diag_solve<X>(ctx, h->lv[t].A<X>(), rt, xt);
+  }
+  for (int l = t - 1; l >= 0; --l) {
+    Level& L = h->lv[l];
+    X* x = l == 0 ? x0 : lvx<X>(h, l);
+    const X* r = l == 0 ? r0 : lvr<X>(h, l);
+    CSRView<PV> T{L.n, L.trp.get(), L.tci.get(), nullptr, L.tvec};
+    if constexpr (std::is_same<PV, double>::value) T.vals = L.tva.get();
+    else T.vals = L.tva16.get();
+    spmv<PV, X>(ctx, T, lvx<X>(h, l + 1), x, true);
+    smooth<X>(h, l, x, r, h->opts.symmetric != 0);
+  }
+}
+
+// Captures (once) and replays the preconditioner z = V(r) on the solver's
+// own level-0 buffers: FP64 on (r, z), mixed on (r32, z32).
+void precondition(afp_amg* h) {
+  afp_context* ctx = h->ctx;
+  const bool mixed = h->opts.precision == AFP_PRECISION_MIXED;
+  cudaGraphExec_t& exec = mixed ? h->graph32 : h->graph64;
+  int64_t& nodes = mixed ? h->graph32_nodes : h->graph64_nodes;
+  if (exec == nullptr) {
+    cudaGraph_t g;
+    const int64_t before = ctx->launches.n;
+    AFP_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      if (mixed) vcycle<float, __nv_bfloat16>(h, h->z32.get(), h->r32.get(), true);
+      else vcycle<double, double>(h, h->z.get(), h->r.get(), true);
+    } catch (...) {
+      cudaStreamEndCapture(ctx->stream, &g);
+      throw;
+    }
+    AFP_CUDA(cudaStreamEndCapture(ctx->stream, &g));
+    AFP_CUDA(cudaGraphInstantiate(&exec, g, 0));
+    AFP_CUDA(cudaGraphDestroy(g));
+    nodes = ctx->launches.n - before;
+    ctx->launches.n = before;
+  }
+  if (mixed) convert<double, float>(ctx, h->lv[0].n, h->r.get(), h->r32.get());
+  AFP_CUDA(cudaGraphLaunch(exec, ctx->stream));
+  ctx->launches.n += nodes;
+  if (mixed) convert<float, double>(ctx, h->lv[0].n, h->z32.get(), h->z.get());
+}
+
+__global__ void k_abs_residual_sum(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci,
+                                   const double* __restrict__ va, const double* __restrict__ x,
+                                   const double* __restrict__ r, double* __restrict__ out) {
+  // out[i] = |(A x)_i - r_i| (then summed by dot with ones)
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  double s = 0;
+  for (int k = rp[i]; k < rp[i + 1]; ++k) s += va[k] * x[ci[k]];
+  out[i] = fabs(s - r[i]);
+}
+
+__global__ void k_fill(int64_t n, double v, double* __restrict__ x) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = v;
+}
+
+double l1_residual(afp_amg* h, const double* x, const double* r) {
+  afp_context* ctx = h->ctx;
+  const Level& L = h->lv[0];
+  k_abs_residual_sum<<<grid_for(L.n, 256), 256, 0, ctx->stream>>>(L.n, L.rp.get(), L.ci.get(), L.va.get(), x, r,
+                                                                  h->tmp.get());
+  check_launch(ctx, "abs residual");
+  k_fill<<<grid_for(L.n, 256), 256, 0, ctx->stream>>>(L.n, 1.0, h->q.get());
+  check_launch(ctx, "ones");
+  dot(ctx, L.n, h->tmp.get(), h->q.get(), ctx->d_scalars + 10);
+  double v;
+  copy(ctx, &v, ctx->d_scalars + 10, sizeof(double));
+  sync(ctx);
+  return v;
+}
+
+void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matrix* A0) {
+  afp_context* ctx = h->ctx;
+  const int t = h->t;
+  const bool mixed = h->opts.precision == AFP_PRECISION_MIXED;
+  h->lv.resize(t + 1);
+  std::vector<std::vector<int>> perm(t + 1), iperm(t + 1);
+  for (int l = 0; l <= t; ++l) {
+    const HostCSR& H = h->refA[l];
+    const int64_t n = H.m;
+    perm[l].resize(n);
+    iperm[l].resize(n);
+    Level& L = h->lv[l];
+    L.n = n;
+    L.nnz = H.nnz();
+    if (l < t) {
+      std::vector<int> color;
+      int K = host_color(H, h->opts.max_colors, color);
+      const int nclass = K;
+      std::vector<int64_t> cnt(nclass + 1, 0);
+      for (int64_t i = 0; i < n; ++i) cnt[color[i] + 1]++;
+      for (int c = 0; c < nclass; ++c) cnt[c + 1] += cnt[c];
+      L.cls.assign(cnt.begin(), cnt.end());
+      L.overflow = (K == h->opts.max_colors + 1);
+      std::vector<int64_t> cur(cnt.begin(), cnt.end() - 1);
+      for (int64_t i = 0; i < n; ++i) perm[l][cur[color[i]]++] = (int)i;
+    } else {
+      std::iota(perm[l].begin(), perm[l].end(), 0);
+      L.cls = {0, n};
+    }
+    for (int64_t i = 0; i < n; ++i) iperm[l][perm[l][i]] = (int)i;
+  }
+  for (int l = 0; l <= t; ++l) {
+    Level& L = h->lv[l];
+    const int* rp = l == 0 ? A0->pat->rowptr.get() : refDev[l].rp.get();
+    const int* ci = l == 0 ? A0->pat->cols.get() : refDev[l].ci.get();
+    const double* va = l == 0 ? A0->vals.get() : refDev[l].va.get();
+    DevBuf<int> dperm(ctx, L.n), diperm(ctx, L.n);
+    dperm.upload(perm[l].data(), L.n);
+    diperm.upload(iperm[l].data(), L.n);
+    permute_csr(ctx, L.n, rp, ci, va, dperm.get(), diperm.get(), L.nnz, L.rp, L.ci, L.va);
+    L.vec = pick_vec((double)L.nnz / (double)L.n);
+    L.perm = std::move(dperm);
+    if (l < t && L.overflow) {
+      const int K = (int)L.cls.size() - 1;
+      const int64_t r0 = L.cls[K - 1], r1 = L.cls[K];
+      L.l1d.alloc(ctx, std::max<int64_t>(1, r1 - r0));
+      l1_diag(ctx, L.A<double>(), r0, r1, L.l1d.get());
+      if (mixed) {
+        L.l1d32.alloc(ctx, std::max<int64_t>(1, r1 - r0));
+        convert<double, float>(ctx, r1 - r0, L.l1d.get(), L.l1d32.get());
+      }
+    }
+    if (mixed) {
+      L.va32.alloc(ctx, L.nnz);
+      convert<double, float>(ctx, L.nnz, L.va.get(), L.va32.get());
+    }
+    if (l > 0 || true) {
+      L.x.alloc(ctx, L.n);
+      L.r.alloc(ctx, L.n);
+      L.tmp.alloc(ctx, L.n);
+      if (mixed) {
+        L.x32.alloc(ctx, L.n);
+        L.r32.alloc(ctx, L.n);
+        L.tmp32.alloc(ctx, L.n);
+      }
+    }
+    (void)diperm;
+  }
+  // projections in the permuted numbering
+  for (int l = 0; l < t; ++l) {
+    Level& L = h->lv[l];
+    const HostCSR& P = h->refP[l];
+    HostCSR Pt;
+    // transpose on the host (cheap: P has few entries per row)
+    Pt.m = P.n;
+    Pt.n = P.m;
+    Pt.rowptr.assign(P.n + 1, 0);
+    for (int q = 0; q < P.nnz(); ++q) Pt.rowptr[P.cols[q] + 1]++;
+    for (int64_t i = 0; i < P.n; ++i) Pt.rowptr[i + 1] += Pt.rowptr[i];
+    Pt.cols.resize(P.nnz());
+    Pt.vals.resize(P.nnz());
+    {
+      std::vector<int> cur(Pt.rowptr.begin(), Pt.rowptr.end() - 1);
+      for (int64_t c = 0; c < P.m; ++c)
+        for (int q = P.rowptr[c]; q < P.rowptr[c + 1]; ++q) {
+          const int k = cur[P.cols[q]]++;
+          Pt.cols[k] = (int)c;
+          Pt.vals[k] = P.vals[q];
+        }
+    }
+    DevCSR dP, dT;
+    upload_host_csr(ctx, P, dP);
+    upload_host_csr(ctx, Pt, dT);
+    DevBuf<int> pr(ctx, P.m), ic(ctx, P.n), tr(ctx, P.n), itc(ctx, P.m);
+    pr.upload(perm[l + 1].data(), P.m);
+    ic.upload(iperm[l].data(), P.n);
+    tr.upload(perm[l].data(), P.n);
+    itc.upload(iperm[l + 1].data(), P.m);
+    permute_csr(ctx, P.m, dP.rp.get(), dP.ci.get(), dP.va.get(), pr.get(), ic.get(), P.nnz(), L.prp, L.pci, L.pva);
+    permute_csr(ctx, P.n, dT.rp.get(), dT.ci.get(), dT.va.get(), tr.get(), itc.get(), P.nnz(), L.trp, L.tci, L.tva);
+    L.pnnz = P.nnz();
+    L.pvec = pick_vec((double)P.nnz() / (double)P.m);
+    L.tvec = pick_vec((double)P.nnz() / (double)P.n);
+    if (mixed) {
+      L.pva16.alloc(ctx, P.nnz());
+      L.tva16.alloc(ctx, P.nnz());
+      convert<double, __nv_bfloat16>(ctx, P.nnz(), L.pva.get(), L.pva16.get());
+      convert<double, __nv_bfloat16>(ctx, P.nnz(), L.tva.get(), L.tva16.get());
+    }
+    sync(ctx);
+  }
+  // tail
+  Level& T = h->lv[t];
+  if (h->tail_dense) {
+    h->tail_inv.alloc(ctx, T.n * T.n);
+    if (!dense_inverse(ctx, T.A<double>(), h->tail_inv.get()))
+      fail(AFP_ERR_SINGULAR, "coarsest matrix is singular");
+    if (mixed) {
+      h->tail_inv32.alloc(ctx, T.n * T.n);
+      convert<double, float>(ctx, T.n * T.n, h->tail_inv.get(), h->tail_inv32.get());
+    }
+  }
+  if (mixed && !h->tail_dense) {
+    T.va32.alloc(ctx, T.nnz);
+    convert<double, float>(ctx, T.nnz, T.va.get(), T.va32.get());
+  }
+  const int64_t n0 = h->lv[0].n;
+  h->b.alloc(ctx, n0);
+  h->x.alloc(ctx, n0);
+  h->r.alloc(ctx, n0);
+  h->z.alloc(ctx, n0);
+  h->p.alloc(ctx, n0);
+  h->q.alloc(ctx, n0);
+  h->tmp.alloc(ctx, n0);
+  if (mixed) {
+    h->r32.alloc(ctx, n0);
+    h->z32.alloc(ctx, n0);
+  }
+  sync(ctx);
+}
+
+void setup(afp_amg* h, afp_matrix* A) {
+  afp_context* ctx = h->ctx;
+  const afp_amg_opts& o = h->opts;
+  AFP_REQUIRE(A->pat->m == A->pat->n, AFP_ERR_INVALID, "matrix is not square");
+  HostCSR H0;
+  download_host_csr(ctx, A->pat->m, A->pat->n, A->pat->nnz, A->pat->rowptr.get(), A->pat->cols.get(), A->vals.get(),
+                    H0);
+  h->refA.push_back(std::move(H0));
+  std::vector<DevCSR> refDev(1);  // refDev[0] unused: the input matrix
+  uint64_t k = (uint64_t)A->pat->m, m = k;
+  float sparse_degree = (float)A->pat->nnz / ((float)m * m);
+  h->most_full = true;
+  int l = 0;
+  while (m > (uint64_t)o.max_coarse || sparse_degree < o.min_density) {
+    if (o.dense_tail > 0 && l > 0 && m <= (uint64_t)o.dense_tail) break;  // the dense tail starts here
+    const HostCSR& M = h->refA[l];
+    std::vector<int> cf;
+    HostCSR P, Pt;
+    host_project(M, o.alpha, cf, P, Pt);
+    DevCSR dP, dT;
+    upload_host_csr(ctx, P, dP);
+    upload_host_csr(ctx, Pt, dT);
+    const int* arp = l == 0 ? A->pat->rowptr.get() : refDev[l].rp.get();
+    const int* aci = l == 0 ? A->pat->cols.get() : refDev[l].ci.get();
+    const double* ava = l == 0 ? A->vals.get() : refDev[l].va.get();
+    Pattern cpat;
+    DevBuf<double> cvals;
+    galerkin_product(ctx, P.m, P.n, dP.rp.get(), dP.ci.get(), dP.va.get(), arp, aci, ava, dT.rp.get(), dT.ci.get(),
+                     dT.va.get(), cpat, cvals);
+    HostCSR C;
+    download_host_csr(ctx, cpat.m, cpat.n, cpat.nnz, cpat.rowptr.get(), cpat.cols.get(), cvals.get(), C);
+    m = (uint64_t)C.m;
+    if (k == m) {
+      h->most_full = false;
+      break;
+    }
+    k = m;
+    DevCSR dc;
+    dc.m = cpat.m;
+    dc.n = cpat.n;
+    dc.nnz = cpat.nnz;
+    dc.rp = std::move(cpat.rowptr);
+    dc.ci = std::move(cpat.cols);
+    dc.va = std::move(cvals);
+    refDev.push_back(std::move(dc));
+    h->refP.push_back(std::move(P));
+    sparse_degree = (float)C.nnz() / ((float)m * m);
+    h->refA.push_back(std::move(C));
+    ++l;
+  }
+  h->n_project = l;
+  h->t = l;
+  h->tail_dense = h->most_full;
+  build_solve_layout(h, refDev, A);
+}
+
+void check_finite(double v, const char* what) {
+  if (!std::isfinite(v)) fail(AFP_ERR_BREAKDOWN, std::string("non-finite ") + what);
+}
+
+void pcg(afp_amg* h, double* x_user, const double* b_user, double tol, int maxit, afp_solve_info* info) {
+  afp_context* ctx = h->ctx;
+  const Level& L0 = h->lv[0];
+  const int64_t n = L0.n;
+  double* s = ctx->d_scalars;
+  cudaEvent_t e0, e1;
+  AFP_CUDA(cudaEventCreate(&e0));
+  AFP_CUDA(cudaEventCreate(&e1));
+  // inputs into solve order
+  copy(ctx, h->tmp.get(), b_user, sizeof(double) * n);
+  AFP_CUDA(cudaEventRecord(e0, ctx->stream));
+  permute_gather(ctx, n, L0.perm.get(), h->tmp.get(), h->b.get());
+  copy(ctx, h->tmp.get(), x_user, sizeof(double) * n);
+  permute_gather(ctx, n, L0.perm.get(), h->tmp.get(), h->x.get());
+  const CSRView<double> A = L0.A<double>();
+  residual<double>(ctx, A, h->x.get(), h->b.get(), h->r.get());
+  dot(ctx, n, h->b.get(), h->b.get(), s + 4);
+  dot(ctx, n, h->r.get(), h->r.get(), s + 2);
+  double hs[5];
+  copy(ctx, hs, s, sizeof(double) * 5);
+  sync(ctx);
+  const double bn = std::max(std::sqrt(hs[4]), 1e-30);
+  double rel = std::sqrt(hs[2]) / bn;
+  check_finite(rel, "initial residual");
+  const double init = rel;
+  int it = 0;
+  bool conv = rel <= tol;
+  if (!conv) {
+    precondition(h);  // z = M r
+    dot(ctx, n, h->r.get(), h->z.get(), s + 0);
+    AFP_CUDA(cudaMemcpyAsync(h->p.get(), h->z.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    int cur = 0, nxt = 3;
+    for (it = 1; it <= maxit; ++it) {
+      spmv_dot(ctx, A, h->p.get(), h->q.get(), s + 1);
+      cg_update_xr(ctx, n, s, cur, 1, h->x.get(), h->r.get(), h->p.get(), h->q.get(), s + 2);
+      double rr;
+      copy(ctx, &rr, s + 2, sizeof(double));
+      sync(ctx);
+      rel = std::sqrt(rr) / bn;
+      check_finite(rel, "residual");
+      if (rel <= tol) {
+        conv = true;
+        break;
+      }
+      precondition(h);
+      dot(ctx, n, h->r.get(), h->z.get(), s + nxt);
+      cg_update_p(ctx, n, s, nxt, cur, h->z.get(), h->p.get());
+      std::swap(cur, nxt);
+    }
+    if (it > maxit) it = maxit;
+  }
+  permute_scatter(ctx, n, L0.perm.get(), h->x.get(), h->tmp.get());
+  AFP_CUDA(cudaEventRecord(e1, ctx->stream));
+  copy(ctx, x_user, h->tmp.get(), sizeof(double) * n);
+  sync(ctx);
+  float ms = 0;
+  AFP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (info) {
+    info->iterations = it;
+    info->converged = conv;
+    info->initial_residual = init;
+    info->final_residual = rel;
+    info->seconds = ms * 1e-3;
+  }
+}
+
+}  // namespace
+}  // namespace afp
+
+extern "C" {
+
+void afp_amg_default_opts(afp_amg_opts* o) {
+  if (!o) return;
+  o->tolerance = 1.0e-12;
+  o->smooth_step = 3;
+  o->max_coarse = 50;
+  o->min_density = 0.382;
+  o->alpha = 0.25;
+  o->precision = AFP_PRECISION_FP64;
+  o->dense_tail = 1024;
+  o->max_colors = 32;
+  o->symmetric = 1;
+}
+
+afp_status afp_amg_setup(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out) {
+  return guarded([&] {
+    AFP_REQUIRE(a && out, AFP_ERR_INVALID, "null argument");
+    bind(a->ctx);
+    auto h = std::make_unique<afp_amg>();
+    h->ctx = a->ctx;
+    if (opts) h->opts = *opts;
+    else afp_amg_default_opts(&h->opts);
+    const afp_amg_opts& o = h->opts;
+    AFP_REQUIRE(o.smooth_step >= 0 && o.max_coarse >= 1 && o.alpha >= 0 && o.max_colors >= 1 && o.dense_tail >= 0 &&
+                    (o.precision == AFP_PRECISION_FP64 || o.precision == AFP_PRECISION_MIXED),
+                AFP_ERR_INVALID, "invalid AMG options");
+    AFP_REQUIRE(o.dense_tail <= 8192, AFP_ERR_UNSUPPORTED, "dense_tail above 8192 rows");
+    setup(h.get(), a);
+    *out = h.release();
+  });
+}
+
+afp_status afp_amg_destroy(afp_amg* h) {
+  return guarded([&] {
+    if (!h) return;
+    bind(h->ctx);
+    sync(h->ctx);
+    delete h;
+  });
+}
+
+afp_status afp_amg_num_levels(const afp_amg* h, int* n_project, int* solve_levels) {
+  return guarded([&] {
+    AFP_REQUIRE(h, AFP_ERR_INVALID, "null solver");
+    if (n_project) *n_project = h->n_project;
+    if (solve_levels) *solve_levels = h->t + 1;
+  });
+}
+
+afp_status afp_amg_level_info(const afp_amg* h, int level, int64_t* n, int64_t* nnz, int* colors) {
+  return guarded([&] {
+    AFP_REQUIRE(h && level >= 0 && level <= h->t, AFP_ERR_INVALID, "bad level");
+    const Level& L = h->lv[level];
+    if (n) *n = L.n;
+    if (nnz) *nnz = L.nnz;
+    if (colors) *colors = level < h->t ? (int)L.cls.size() - 1 : -1;
+  });
+}
+
+afp_status afp_amg_download_level(const afp_amg* h, int level, int32_t* rowptr, int32_t* cols, double* vals) {
+  return guarded([&] {
+    AFP_REQUIRE(h && level >= 0 && level <= h->n_project, AFP_ERR_INVALID, "bad level");
+    const HostCSR& H = h->refA[level];
+    if (rowptr) std::copy(H.rowptr.begin(), H.rowptr.end(), rowptr);
+    if (cols) std::copy(H.cols.begin(), H.cols.end(), cols);
+    if (vals) std::copy(H.vals.begin(), H.vals.end(), vals);
+  });
+}
+
+afp_status afp_amg_download_projection(const afp_amg* h, int level, int32_t* rowptr, int32_t* cols, double* vals) {
+  return guarded([&] {
+    AFP_REQUIRE(h && level >= 0 && level < h->n_project, AFP_ERR_INVALID, "bad level");
+    const HostCSR& H = h->refP[level];
+    if (rowptr) std::copy(H.rowptr.begin(), H.rowptr.end(), rowptr);
+    if (cols) std::copy(H.cols.begin(), H.cols.end(), cols);
+    if (vals) std::copy(H.vals.begin(), H.vals.end(), vals);
+  });
+}
+
+afp_status afp_amg_solve(afp_amg* h, double* x, const double* r, double tol, int64_t step, int mode,
+                         afp_solve_info* info) {
+  return guarded([&] {
+    AFP_REQUIRE(h && x && r && step >= 0, AFP_ERR_INVALID, "bad argument");
+    (void)mode;
+    afp_context* ctx = h->ctx;
+    bind(ctx);
+    if (tol == 0.0) tol = h->opts.tolerance;
+    const Level& L0 = h->lv[0];
+    const int64_t n = L0.n;
+    cudaEvent_t e0, e1;
+    AFP_CUDA(cudaEventCreate(&e0));
+    AFP_CUDA(cudaEventCreate(&e1));
+    copy(ctx, h->tmp.get(), r, sizeof(double) * n);
+    AFP_CUDA(cudaEventRecord(e0, ctx->stream));
+    permute_gather(ctx, n, L0.perm.get(), h->tmp.get(), h->b.get());
+    copy(ctx, h->tmp.get(), x, sizeof(double) * n);
+    permute_gather(ctx, n, L0.perm.get(), h->tmp.get(), h->x.get());
+    const double init = l1_residual(h, h->x.get(), h->b.get());
+    for (int64_t it = 0; it <= step; ++it) {
+      // x <- x + V(b - A x): the same iterate as a V-cycle started from x
+      residual<double>(ctx, L0.A<double>(), h->x.get(), h->b.get(), h->r.get());
+      precondition(h);
+      axpy(ctx, n, 1.0, h->z.get(), h->x.get());
+    }
+    const double fin = l1_residual(h, h->x.get(), h->b.get());
+    permute_scatter(ctx, n, L0.perm.get(), h->x.get(), h->tmp.get());
+    AFP_CUDA(cudaEventRecord(e1, ctx->stream));
+    copy(ctx, x, h->tmp.get(), sizeof(double) * n);
+    sync(ctx);
+    float ms = 0;
+    AFP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (info) {
+      info->iterations = (int)(step + 1);
+      info->converged = fin < tol * init;
+      info->initial_residual = init;
+      info->final_residual = fin;
+      info->seconds = ms * 1e-3;
+    }
+  });
+}
+
+afp_status afp_amg_precondition(afp_amg* h, double* x, const double* b, int iterate_step) {
+  return afp_amg_solve(h, x, b, 0.0, iterate_step, 1, nullptr);
+}
+
+afp_status afp_pcg_solve(afp_amg* h, double* x, const double* b, double tol, int maxit, afp_solve_info* info) {
+  return guarded([&] {
+    AFP_REQUIRE(h && x && b && maxit >= 0 && tol >= 0, AFP_ERR_INVALID, "bad argument");
+    bind(h->ctx);
+    pcg(h, x, b, tol, maxit, info);
+  });
+}
+
+afp_status afp_pcg_solve_multi(afp_amg* h, double* X, const double* B, int nrhs, double tol, int maxit,
+                               afp_solve_info* info) {
+  return guarded([&] {
+    AFP_REQUIRE(h && X && B && nrhs > 0, AFP_ERR_INVALID, "bad argument");
+    afp_context* ctx = h->ctx;
+    bind(ctx);
+    const int64_t n = h->lv[0].n;
+    DevBuf<double> dB(ctx, n * nrhs), dX(ctx, n * nrhs), xc(ctx, n), bc(ctx, n);
+    dB.upload(B, n * nrhs);
+    dX.upload(X, n * nrhs);
+    for (int k = 0; k < nrhs; ++k) {
+      strided_copy(ctx, n, dB.get() + k, nrhs, bc.get(), 1);
+      strided_copy(ctx, n, dX.get() + k, nrhs, xc.get(), 1);
+      pcg(h, xc.get(), bc.get(), tol, maxit, info ? info + k : nullptr);
+      strided_copy(ctx, n, xc.get(), 1, dX.get() + k, nrhs);
+    }
+    dX.download(X, n * nrhs);
+    sync(ctx);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,249 @@
+// Host side of the AMG setup: the reference's C/F splitting and projection
+// (AMGSolver::Project, src/AMGSolver.cpp:18-226) and the greedy colouring
+// that orders the GPU smoother.
+//
+// Project runs on the host by design (it is a sequential greedy sweep over
+// the rows).  This implementation keeps the reference's decisions and
+// floating-point operations -- the same strength threshold, the same
+// row-order greedy passes, the same weight formulas accumulated in the same
+// order -- so C/F flags and P are bitwise the reference's.  It replaces the
+// reference's linear scans (SparseMatrix::el, std::find, SparsityPattern::add)
+// by binary searches on the sorted rows, which return the same entries.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace afp {
+
+namespace {
+
+// value of (i, j) in a [diag, ascending others] row, 0 when absent
+inline double entry(const HostCSR& M, int i, int j) {
+  const int b = M.rowptr[i], e = M.rowptr[i + 1];
+  if (b == e) return 0.0;
+  if (M.cols[b] == j) return M.vals[b];
+  const int* lo = M.cols.data() + b + 1;
+  const int* hi = M.cols.data() + e;
+  const int* p = std::lower_bound(lo, hi, j);
+  return (p != hi && *p == j) ? M.vals[p - M.cols.data()] : 0.0;
+}
+
+inline bool sorted_contains(const int* b, const int* e, int key) {
+  const int* p = std::lower_bound(b, e, key);
+  return p != e && *p == key;
+}
+
+}  // namespace
+
+void host_project(const HostCSR& M, double alpha, std::vector<int>& flag, HostCSR& P, HostCSR& Pt) {
+  const int m = (int)M.m;
+  const int* rs = M.rowptr.data();
+  const int* cn = M.cols.data();
+  const double* v = M.vals.data();
+  flag.assign(m, 0);
+  std::vector<double> beta(m, 0.0);
+  int n_core = 0;
+  // first pass: thresholds and greedy C-point choice in row order
+  for (int i = 0; i < m; ++i) {
+    double b = 0.0;
+    for (int j = rs[i] + 1; j < rs[i + 1]; ++j) {
+      const double a = std::fabs(v[j]);
+      b = (a < b) ? b : a;
+    }
+    beta[i] = b * alpha;
+    if (flag[i] != 0) continue;
+    for (int j = rs[i] + 1; j < rs[i + 1]; ++j) {
+      const int k = cn[j];
+      if (flag[k] == -1) continue;
+      if (std::fabs(v[j]) < beta[i]) continue;
+      flag[k] = 1;
+    }
+    flag[i] = -1;
+    ++n_core;
+  }
+  // second pass: F points with a strong F-F connection lacking a common
+  // strong C neighbour become C points
+  std::vector<int> dep;
+  for (int i = 0; i < m; ++i) {
+    if (flag[i] != 1) continue;
+    dep.clear();
+    for (int j = rs[i] + 1; j < rs[i + 1]; ++j) {
+      if (std::fabs(v[j]) < beta[i]) continue;
+      if (flag[cn[j]] == -1) dep.push_back(cn[j]);
+    }
+    bool is_FF = false;
+    for (int j = rs[i] + 1; j < rs[i + 1]; ++j) {
+      const int k = cn[j];
+      if (flag[k] == -1 || k < i || std::fabs(v[j]) < beta[i]) continue;
+      is_FF = true;
+      for (int j1 = rs[k] + 1; j1 < rs[k + 1]; ++j1) {
+        const int k1 = cn[j1];
+        if (flag[k1] != -1) continue;
+        if (std::find(dep.begin(), dep.end(), k1) != dep.end()) {
+          is_FF = false;
+          break;
+        }
+      }
+      if (is_FF) break;
+    }
+    if (!is_FF) continue;
+    flag[i] = -1;
+    ++n_core;
+  }
+  std::vector<int> core_point(n_core), core_at(m, -1);
+  for (int i = 0, n = 0; i < m; ++i)
+    if (flag[i] == -1) {
+      core_point[n] = i;
+      core_at[i] = n++;
+    }
+  // pattern of P: row c = {core point} U {its non-C neighbours}, ascending
+  // (rectangular SparsityPattern rows are fully sorted by compress)
+  P.m = n_core;
+  P.n = m;
+  P.rowptr.assign(n_core + 1, 0);
+  for (int c = 0; c < n_core; ++c) {
+    const int k = core_point[c];
+    int len = 1;
+    for (int j = rs[k] + 1; j < rs[k + 1]; ++j) len += (flag[cn[j]] != -1);
+    P.rowptr[c + 1] = P.rowptr[c] + len;
+  }
+  P.cols.resize(P.rowptr[n_core]);
+  for (int c = 0; c < n_core; ++c) {
+    const int k = core_point[c];
+    int* out = P.cols.data() + P.rowptr[c];
+    int q = 0;
+    bool placed = false;
+    for (int j = rs[k] + 1; j < rs[k + 1]; ++j) {
+      const int l = cn[j];
+      if (flag[l] == -1) continue;
+      if (!placed && l > k) {
+        out[q++] = k;
+        placed = true;
+      }
+      out[q++] = l;
+    }
+    if (!placed) out[q++] = k;
+  }
+  if (n_core == m) {
+    // square case: SparsityPattern keeps the diagonal first (all points are C)
+    for (int c = 0; c < n_core; ++c) P.cols[P.rowptr[c]] = c;
+  }
+  // Pt = transpose pattern, rows ascending in the coarse index
+  Pt.m = m;
+  Pt.n = n_core;
+  Pt.rowptr.assign(m + 1, 0);
+  for (int q = 0; q < P.rowptr[n_core]; ++q) Pt.rowptr[P.cols[q] + 1]++;
+  for (int i = 0; i < m; ++i) Pt.rowptr[i + 1] += Pt.rowptr[i];
+  Pt.cols.resize(P.rowptr[n_core]);
+  {
+    std::vector<int> cur(Pt.rowptr.begin(), Pt.rowptr.end() - 1);
+    for (int c = 0; c < n_core; ++c)
+      for (int q = P.rowptr[c]; q < P.rowptr[c + 1]; ++q) Pt.cols[cur[P.cols[q]]++] = c;
+  }
+  // weights, accumulated per fine point in the reference's order
+  Pt.vals.assign(Pt.cols.size(), 0.0);
+  auto add_pt = [&](int i, int c, double w) {
+    const int* b = Pt.cols.data() + Pt.rowptr[i];
+    const int* e = Pt.cols.data() + Pt.rowptr[i + 1];
+    const int* p = std::lower_bound(b, e, c);
+    if (p != e && *p == c) Pt.vals[p - Pt.cols.data()] += w;
+  };
+  for (int i = 0; i < m; ++i) {
+    const int k = core_at[i];
+    if (k >= 0) {
+      add_pt(i, k, 1.0);
+      continue;
+    }
+    double aii = v[rs[i]];
+    for (int j = rs[i] + 1; j < rs[i + 1]; ++j)
+      if (std::fabs(v[j]) < beta[i]) aii += v[j];
+    const int* dep_b = Pt.cols.data() + Pt.rowptr[i];
+    const int* dep_e = Pt.cols.data() + Pt.rowptr[i + 1];
+    for (int j = rs[i] + 1; j < rs[i + 1]; ++j) {
+      const int l = cn[j];
+      if (std::fabs(v[j]) < beta[i]) continue;
+      if (core_at[l] >= 0) {
+        add_pt(i, core_at[l], std::fabs(v[j] / aii));
+      } else {
+        double d = 0.0;
+        for (int i1 = Pt.rowptr[l]; i1 < Pt.rowptr[l + 1]; ++i1) {
+          const int c1 = Pt.cols[i1];
+          if (sorted_contains(dep_b, dep_e, c1)) d += entry(M, l, core_point[c1]);
+        }
+        if (std::fabs(d * aii) < 1e-16) continue;
+        for (int i1 = Pt.rowptr[l]; i1 < Pt.rowptr[l + 1]; ++i1) {
+          const int c1 = Pt.cols[i1];
+          if (sorted_contains(dep_b, dep_e, c1))
+            add_pt(i, c1, std::fabs(entry(M, i, l) * entry(M, l, core_point[c1]) / (d * aii)));
+        }
+      }
+    }
+  }
+  // P values: P(c, i) received the same additions as Pt(i, c)
+  P.vals.assign(P.cols.size(), 0.0);
+  {
+    std::vector<int> cur(P.rowptr.begin(), P.rowptr.end() - 1);
+    for (int i = 0; i < m; ++i)
+      for (int q = Pt.rowptr[i]; q < Pt.rowptr[i + 1]; ++q) {
+        const int c = Pt.cols[q];
+        // P rows are ascending in the fine index and i ascends here
+        P.vals[cur[c]++] = Pt.vals[q];
+      }
+  }
+}
+
+int host_color(const HostCSR& A, int max_colors, std::vector<int>& color) {
+  const int m = (int)A.m;
+  color.assign(m, -1);
+  std::vector<int> mark(max_colors + 1, -1);
+  int used = 0;
+  bool overflow = false;
+  for (int i = 0; i < m; ++i) {
+    for (int q = A.rowptr[i] + 1; q < A.rowptr[i + 1]; ++q) {
+      const int k = A.cols[q];
+      if (color[k] < 0) continue;
+      if (A.vals[q] == 0.0 && entry(A, k, i) == 0.0) continue;  // no coupling either way
+      mark[color[k]] = i;
+    }
+    int c = 0;
+    while (c < max_colors && mark[c] == i) ++c;
+    color[i] = c;  // c == max_colors is the overflow class
+    if (c == max_colors) overflow = true;
+    else used = std::max(used, c + 1);
+  }
+  return overflow ? max_colors + 1 : used;
+}
+
+}  // namespace afp
+
+using namespace afp;
+
+extern "C" afp_status afp_host_coarsen(int64_t m, const int32_t* rowptr, const int32_t* cols, const double* vals,
+                                       double alpha, int32_t* cf, int64_t* n_coarse, int32_t** p_rowptr,
+                                       int32_t** p_cols, double** p_vals) {
+  return guarded([&] {
+    AFP_REQUIRE(m > 0 && rowptr && cols && vals && n_coarse && p_rowptr && p_cols && p_vals, AFP_ERR_INVALID,
+                "null argument");
+    HostCSR M;
+    M.m = M.n = m;
+    M.rowptr.assign(rowptr, rowptr + m + 1);
+    M.cols.assign(cols, cols + rowptr[m]);
+    M.vals.assign(vals, vals + rowptr[m]);
+    std::vector<int> flag;
+    HostCSR P, Pt;
+    host_project(M, alpha, flag, P, Pt);
+    if (cf) std::memcpy(cf, flag.data(), sizeof(int) * m);
+    *n_coarse = P.m;
+    *p_rowptr = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * (P.m + 1)));
+    *p_cols = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * std::max<size_t>(1, P.cols.size())));
+    *p_vals = static_cast<double*>(std::malloc(sizeof(double) * std::max<size_t>(1, P.vals.size())));
+    AFP_REQUIRE(*p_rowptr && *p_cols && *p_vals, AFP_ERR_OUT_OF_MEMORY, "host allocation failed");
+    std::memcpy(*p_rowptr, P.rowptr.data(), sizeof(int32_t) * (P.m + 1));
+    std::memcpy(*p_cols, P.cols.data(), sizeof(int32_t) * P.cols.size());
+    std::memcpy(*p_vals, P.vals.data(), sizeof(double) * P.vals.size());
+  });
+}

@@ -1,0 +1,37 @@
+// Declarations shared between the library's translation units.
+#pragma once
+
+#include "common.cuh"
+
+namespace afp {
+
+// y = A x over a CSR (any row order); one launch.
+void csr_spmv(const afp_context* ctx, int64_t m, const int* rowptr, const int* cols, const double* vals,
+              const double* x, double* y);
+
+// Galerkin product A_c = P A P^T with AFEPack's pattern (diagonal first,
+// then ascending) and getPMPt's accumulation order.  P is n_c x n_f with
+// ascending columns, Pt its transpose with ascending columns.
+void galerkin_product(const afp_context* ctx, int64_t n_c, int64_t n_f, const int* p_rowptr, const int* p_cols,
+                      const double* p_vals, const int* a_rowptr, const int* a_cols, const double* a_vals,
+                      const int* pt_rowptr, const int* pt_cols, const double* pt_vals, Pattern& out_pat,
+                      DevBuf<double>& out_vals);
+
+// Host CSR (AFEPack layout) used by the coarsening.
+struct HostCSR {
+  int64_t m = 0, n = 0;
+  std::vector<int> rowptr, cols;
+  std::vector<double> vals;
+  int64_t nnz() const { return rowptr.empty() ? 0 : rowptr[m]; }
+};
+
+// Project(): C/F splitting and projection P (n_c x m) of one level, with
+// its transpose; cf[i] = -1 (C) or 1 (F).
+void host_project(const HostCSR& M, double alpha, std::vector<int>& cf, HostCSR& P, HostCSR& Pt);
+
+// Greedy colouring of a square matrix's graph (nonzero off-diagonal entries
+// couple rows): colour[i] < max_colors, or max_colors for rows that found no
+// free colour (the overflow class).  Returns the number of classes used.
+int host_color(const HostCSR& A, int max_colors, std::vector<int>& color);
+
+}  // namespace afp

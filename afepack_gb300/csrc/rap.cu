@@ -1,0 +1,294 @@
+// Galerkin coarse operator A_c = P A P^T on the GPU (AMGSolver::getPMPt,
+// src/AMGSolver.cpp:288-358).
+//
+// Symbolic phase: one warp (or, for long rows, one block) per coarse row
+// collects the column set {c : c in Pt[b], b in A[a], a in P[i]} in a
+// shared-memory hash set, then sorts it and writes the row as
+// [i, ascending others] -- the pattern getPMPt builds and compresses.
+//
+// Numeric phase: one warp per coarse row walks the (j, k) pairs of the
+// triple loop in the reference's order (P row ascending, A row in stored
+// order), and the lanes take the entries l of the Pt row, whose columns are
+// distinct, so every output entry receives its products in exactly the
+// reference's order: row_entry[c] += P(i,a)*A(a,b)*Pt(b,c).  Compiled with
+// -fmad=false, the result is bitwise that of getPMPt.
+#include <climits>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace afp {
+namespace {
+
+constexpr int WARP_CAP = 1024;      // hash slots of the warp-level symbolic pass
+constexpr int BLOCK_CAP = 16384;    // hash slots of the block-level pass (2 x 64 KB of shared memory)
+constexpr int ACC_CAP = 1024;       // row length kept in shared memory by the numeric pass
+
+__device__ __forceinline__ unsigned hash_slot(int key, int cap) {
+  return ((unsigned)key * 2654435761u) & (unsigned)(cap - 1);
+}
+
+// Inserts key; returns 1 if it was new.  cap is a power of two.
+__device__ __forceinline__ int hash_insert(int* table, int cap, int key) {
+  unsigned s = hash_slot(key, cap);
+  for (int probe = 0; probe < cap; ++probe) {
+    int prev = atomicCAS(&table[s], -1, key);
+    if (prev == -1) return 1;
+    if (prev == key) return 0;
+    s = (s + 1) & (unsigned)(cap - 1);
+  }
+  return 0;  // table full: caller checks the count against the capacity
+}
+
+template <int GROUP>
+__device__ __forceinline__ void group_bitonic_sort(int* buf, int P, int tid) {
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = tid; t < P; t += GROUP) {
+        int ixj = t ^ j;
+        if (ixj > t) {
+          int a = buf[t], b = buf[ixj];
+          bool up = (t & k) == 0;
+          if ((a > b) == up) {
+            buf[t] = b;
+            buf[ixj] = a;
+          }
+        }
+      }
+      if (GROUP == 32) __syncwarp(); else __syncthreads();
+    }
+  }
+}
+
+// Collects the coarse row's column set with GROUP threads (a warp or a block).
+// Returns the unique count (may exceed 0.75*cap: the caller re-routes the row).
+template <int GROUP>
+__device__ int collect_row(int64_t i, const int* __restrict__ prp, const int* __restrict__ pc,
+                           const int* __restrict__ arp, const int* __restrict__ ac, const int* __restrict__ trp,
+                           const int* __restrict__ tc, int* table, int cap, int tid, int* red) {
+  for (int t = tid; t < cap; t += GROUP) table[t] = -1;
+  if (GROUP == 32) __syncwarp(); else __syncthreads();
+  int mine = 0;
+  const int limit = (cap * 3) / 4;
+  for (int j = prp[i]; j < prp[i + 1]; ++j) {
+    const int a = pc[j];
+    const int kb = arp[a], ke = arp[a + 1];
+    for (int k = kb + tid; k < ke; k += GROUP) {
+      const int b = ac[k];
+      for (int l = trp[b]; l < trp[b + 1]; ++l) mine += hash_insert(table, cap, tc[l]);
+    }
+  }
+  // reduce the count
+  int cnt = mine;
+  if (GROUP == 32) {
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    cnt = __shfl_sync(0xffffffffu, cnt, 0);
+  } else {
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((tid & 31) == 0) atomicAdd(red, cnt);
+    __syncthreads();
+    cnt = *red;
+    __syncthreads();
+  }
+  (void)limit;
+  return cnt;
+}
+
+// Sorts the collected set into `out` as [i, ascending others].
+template <int GROUP>
+__device__ void emit_row(int64_t i, int* table, int* buf, int cap, int cnt, int tid, int* out, int* red) {
+  // compact the table into buf
+  if (GROUP == 32) {
+    int base = 0;
+    for (int t0 = 0; t0 < cap; t0 += 32) {
+      int t = t0 + tid;
+      int key = table[t];
+      bool keep = key >= 0 && key != (int)i;
+      unsigned mask = __ballot_sync(0xffffffffu, keep);
+      if (keep) buf[base + __popc(mask & ((1u << tid) - 1u))] = key;
+      base += __popc(mask);
+    }
+    __syncwarp();
+  } else {
+    if (tid == 0) *red = 0;
+    __syncthreads();
+    for (int t = tid; t < cap; t += GROUP) {
+      int key = table[t];
+      if (key >= 0 && key != (int)i) buf[atomicAdd(red, 1)] = key;
+    }
+    __syncthreads();
+  }
+  const int m = cnt - 1;
+  int P = 1;
+  while (P < m) P <<= 1;
+  for (int t = m + tid; t < P; t += GROUP) buf[t] = INT_MAX;
+  if (GROUP == 32) __syncwarp(); else __syncthreads();
+  group_bitonic_sort<GROUP>(buf, P, tid);
+  if (tid == 0) out[0] = (int)i;
+  for (int t = tid; t < m; t += GROUP) out[1 + t] = buf[t];
+  if (GROUP == 32) __syncwarp(); else __syncthreads();
+}
+
+// Warp-level symbolic pass over all rows.  count mode (rowptr == nullptr):
+// row_len[i] = unique count, or -1 when the row needs the block-level pass.
+__global__ void k_rap_symbolic_warp(int64_t n_c, const int* prp, const int* pc, const int* arp, const int* ac,
+                                    const int* trp, const int* tc, int* row_len, const int* rowptr, int* cols,
+                                    const unsigned char* big_flag) {
+  extern __shared__ int sm_rap[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  int* table = sm_rap + warp * 2 * WARP_CAP;
+  int* buf = table + WARP_CAP;
+  for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < n_c; i += (int64_t)gridDim.x * wpb) {
+    if (rowptr != nullptr && big_flag[i]) continue;  // handled by the block pass
+    int cnt = collect_row<32>(i, prp, pc, arp, ac, trp, tc, table, WARP_CAP, lane, nullptr);
+    if (rowptr == nullptr) {
+      if (lane == 0) row_len[i] = (cnt > (WARP_CAP * 3) / 4) ? -1 : cnt;
+    } else {
+      emit_row<32>(i, table, buf, WARP_CAP, cnt, lane, cols + rowptr[i], nullptr);
+    }
+    __syncwarp();
+  }
+}
+
+// Block-level symbolic pass over the rows listed in `rows`.
+__global__ void k_rap_symbolic_block(const int* rows, int n_rows, int cap, const int* prp, const int* pc,
+                                     const int* arp, const int* ac, const int* trp, const int* tc, int* row_len,
+                                     const int* rowptr, int* cols, int* overflow) {
+  extern __shared__ int sm_rapb[];
+  __shared__ int red;
+  int* table = sm_rapb;
+  int* buf = sm_rapb + cap;
+  for (int r = blockIdx.x; r < n_rows; r += gridDim.x) {
+    const int64_t i = rows[r];
+    if (threadIdx.x == 0) red = 0;
+    __syncthreads();
+    int cnt = collect_row<256>(i, prp, pc, arp, ac, trp, tc, table, cap, threadIdx.x, &red);
+    if (rowptr == nullptr) {
+      if (threadIdx.x == 0) {
+        if (cnt > (cap * 3) / 4) atomicExch(overflow, 1);
+        row_len[i] = cnt;
+      }
+    } else {
+      emit_row<256>(i, table, buf, cap, cnt, threadIdx.x, cols + rowptr[i], &red);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_collect_big(const int* row_len, int64_t n, int* rows, int* count, unsigned char* big_flag) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bool big = row_len[i] < 0;
+  big_flag[i] = big;
+  if (big) rows[atomicAdd(count, 1)] = (int)i;
+}
+
+__device__ __forceinline__ int find_slot(const int* c, int R, int key, int row) {
+  if (key == row) return 0;
+  int lo = 1, hi = R;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (c[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// Numeric pass: exact reference accumulation order (see file comment).
+__global__ void k_rap_numeric(int64_t n_c, const int* __restrict__ prp, const int* __restrict__ pc,
+                              const double* __restrict__ pv, const int* __restrict__ arp, const int* __restrict__ ac,
+                              const double* __restrict__ av, const int* __restrict__ trp, const int* __restrict__ tc,
+                              const double* __restrict__ tv, const int* __restrict__ rowptr,
+                              const int* __restrict__ cols, double* __restrict__ vals) {
+  extern __shared__ __align__(16) unsigned char sm_num[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  double* sacc = reinterpret_cast<double*>(sm_num) + (size_t)warp * ACC_CAP;
+  int* scol = reinterpret_cast<int*>(reinterpret_cast<double*>(sm_num) + (size_t)wpb * ACC_CAP) + warp * ACC_CAP;
+  for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < n_c; i += (int64_t)gridDim.x * wpb) {
+    const int r0 = rowptr[i], R = rowptr[i + 1] - r0;
+    const bool in_smem = R <= ACC_CAP;
+    double* acc = in_smem ? sacc : vals + r0;
+    const int* rc = in_smem ? scol : cols + r0;
+    for (int t = lane; t < R; t += 32) {
+      acc[t] = 0.0;
+      if (in_smem) scol[t] = cols[r0 + t];
+    }
+    __syncwarp();
+    for (int j = prp[i]; j < prp[i + 1]; ++j) {
+      const int a = pc[j];
+      const double p = pv[j];
+      for (int k = arp[a]; k < arp[a + 1]; ++k) {
+        const int b = ac[k];
+        const double pm = p * av[k];
+        for (int l = trp[b] + lane; l < trp[b + 1]; l += 32) {
+          const int slot = find_slot(rc, R, tc[l], (int)i);
+          acc[slot] += pm * tv[l];
+        }
+        __syncwarp();
+      }
+    }
+    if (in_smem)
+      for (int t = lane; t < R; t += 32) vals[r0 + t] = sacc[t];
+    __syncwarp();
+  }
+}
+
+}  // namespace
+
+void galerkin_product(const afp_context* ctx, int64_t n_c, int64_t n_f, const int* prp, const int* pc,
+                      const double* pv, const int* arp, const int* ac, const double* av, const int* trp,
+                      const int* tc, const double* tv, Pattern& out, DevBuf<double>& vals) {
+  (void)n_f;
+  const int wpb = 4;
+  const size_t smem_w = (size_t)wpb * 2 * WARP_CAP * sizeof(int);
+  AFP_CUDA(cudaFuncSetAttribute(k_rap_symbolic_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_w));
+  const unsigned grid = (unsigned)std::min<int64_t>((n_c + wpb - 1) / wpb, (int64_t)ctx->sm_count * 16);
+  DevBuf<int> row_len(ctx, n_c);
+  k_rap_symbolic_warp<<<grid, wpb * 32, smem_w, ctx->stream>>>(n_c, prp, pc, arp, ac, trp, tc, row_len.get(), nullptr,
+                                                               nullptr, nullptr);
+  check_launch(ctx, "rap symbolic count");
+  // rows whose column set does not fit the warp table go to the block pass
+  DevBuf<int> big(ctx, n_c), nbig(ctx, 1), overflow(ctx, 1);
+  DevBuf<unsigned char> big_flag(ctx, n_c);
+  nbig.zero();
+  overflow.zero();
+  k_collect_big<<<grid_for(n_c, 256), 256, 0, ctx->stream>>>(row_len.get(), n_c, big.get(), nbig.get(),
+                                                             big_flag.get());
+  check_launch(ctx, "rap big rows");
+  int hbig = 0;
+  nbig.download(&hbig, 1);
+  sync(ctx);
+  int bcap = 1;
+  while (bcap < 2 * n_c && bcap < BLOCK_CAP) bcap <<= 1;
+  const size_t smem_b = (size_t)2 * bcap * sizeof(int);
+  if (hbig > 0) {
+    AFP_CUDA(cudaFuncSetAttribute(k_rap_symbolic_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
+    k_rap_symbolic_block<<<(unsigned)std::min(hbig, ctx->sm_count * 2), 256, smem_b, ctx->stream>>>(
+        big.get(), hbig, bcap, prp, pc, arp, ac, trp, tc, row_len.get(), nullptr, nullptr, overflow.get());
+    check_launch(ctx, "rap symbolic count (block)");
+    int hov = 0;
+    overflow.download(&hov, 1);
+    sync(ctx);
+    AFP_REQUIRE(!hov, AFP_ERR_UNSUPPORTED, "Galerkin product row longer than the block-level table");
+  }
+  out.m = out.n = n_c;
+  out.rowptr.alloc(ctx, n_c + 1);
+  out.nnz = exclusive_scan(ctx, row_len.get(), out.rowptr.get(), n_c);
+  out.cols.alloc(ctx, out.nnz);
+  if (hbig > 0) {
+    k_rap_symbolic_block<<<(unsigned)std::min(hbig, ctx->sm_count * 2), 256, smem_b, ctx->stream>>>(
+        big.get(), hbig, bcap, prp, pc, arp, ac, trp, tc, row_len.get(), out.rowptr.get(), out.cols.get(),
+        overflow.get());
+    check_launch(ctx, "rap symbolic fill (block)");
+  }
+  k_rap_symbolic_warp<<<grid, wpb * 32, smem_w, ctx->stream>>>(n_c, prp, pc, arp, ac, trp, tc, row_len.get(),
+                                                               out.rowptr.get(), out.cols.get(), big_flag.get());
+  check_launch(ctx, "rap symbolic fill");
+  vals.alloc(ctx, out.nnz);
+  const size_t smem_n = (size_t)wpb * ACC_CAP * (sizeof(double) + sizeof(int));
+  AFP_CUDA(cudaFuncSetAttribute(k_rap_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_n));
+  k_rap_numeric<<<grid, wpb * 32, smem_n, ctx->stream>>>(n_c, prp, pc, pv, arp, ac, av, trp, tc, tv, out.rowptr.get(),
+                                                         out.cols.get(), vals.get());
+  check_launch(ctx, "rap numeric");
+}
+
+}  // namespace afp

@@ -1,0 +1,580 @@
+// Sparse kernels of the V-cycle and the outer CG.
+//
+// Every row kernel assigns a group of VEC consecutive threads to one CSR row
+// (VEC from the level's mean row length), so the row's column numbers and
+// values are read as contiguous, coalesced segments; partial sums are
+// combined with warp shuffles.  Colour classes are contiguous row ranges
+// (the hierarchy is stored colour-permuted), so a Gauss-Seidel class is one
+// launch over a dense range without an index list.
+//
+// Reductions are deterministic: each block writes a partial sum and the last
+// block to finish adds the partials in block order.
+#include "kernels.cuh"
+#include "solve.cuh"
+
+namespace afp {
+
+int pick_vec(double avg) {
+  if (avg <= 4.5) return 4;
+  if (avg <= 10.0) return 8;
+  if (avg <= 20.0) return 16;
+  return 32;
+}
+
+namespace {
+
+constexpr int BLK = 256;
+
+template <class X>
+struct Acc {
+  using type = float;
+};
+template <>
+struct Acc<double> {
+  using type = double;
+};
+
+template <class V>
+__device__ __forceinline__ float tof(V v) {
+  return (float)v;
+}
+template <>
+__device__ __forceinline__ float tof<__nv_bfloat16>(__nv_bfloat16 v) {
+  return __bfloat162float(v);
+}
+
+template <class A, class V>
+__device__ __forceinline__ A val_as(V v) {
+  return (A)v;
+}
+template <>
+__device__ __forceinline__ float val_as<float, __nv_bfloat16>(__nv_bfloat16 v) {
+  return __bfloat162float(v);
+}
+
+template <int VEC, class T>
+__device__ __forceinline__ T group_sum(T s) {
+#pragma unroll
+  for (int o = VEC / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, VEC);
+  return s;
+}
+
+template <int VEC, class V, class X, bool ADD>
+__global__ void k_spmv(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci, const V* __restrict__ va,
+                       const X* __restrict__ x, X* __restrict__ y) {
+  using A = typename Acc<X>::type;
+  const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
+  const int lane = threadIdx.x % VEC;
+  A s = 0;
+  if (g < m)
+    for (int k = rp[g] + lane; k < rp[g + 1]; k += VEC) s += val_as<A>(va[k]) * (A)x[ci[k]];
+  s = group_sum<VEC>(s);
+  if (g < m && lane == 0) y[g] = ADD ? (X)((A)y[g] + s) : (X)s;
+}
+
+template <int VEC, class X>
+__global__ void k_residual(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci, const X* __restrict__ va,
+                           const X* __restrict__ x, const X* __restrict__ r, X* __restrict__ out) {
+  using A = typename Acc<X>::type;
+  const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
+  const int lane = threadIdx.x % VEC;
+  A s = 0;
+  if (g < m)
+    for (int k = rp[g] + lane; k < rp[g + 1]; k += VEC) s += (A)va[k] * (A)x[ci[k]];
+  s = group_sum<VEC>(s);
+  if (g < m && lane == 0) out[g] = (X)((A)r[g] - s);
+}
+
+template <int VEC, class X>
+__global__ void k_gs_class(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
+                           const X* __restrict__ va, X* __restrict__ x, const X* __restrict__ r) {
+  using A = typename Acc<X>::type;
+  const int64_t row = r0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
+  const int lane = threadIdx.x % VEC;
+  A s = 0;
+  int d = 0;
+  if (row < r1) {
+    d = rp[row];
+    for (int k = d + 1 + lane; k < rp[row + 1]; k += VEC) s += (A)va[k] * (A)x[ci[k]];
+  }
+  s = group_sum<VEC>(s);
+  if (row < r1 && lane == 0) x[row] = (X)(((A)r[row] - s) / (A)va[d]);
+}
+
+template <int VEC, class X>
+__global__ void k_jacobi_l1(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
+                            const X* __restrict__ va, const X* __restrict__ x, const X* __restrict__ r,
+                            const X* __restrict__ d, X* __restrict__ tmp) {
+  using A = typename Acc<X>::type;
+  const int64_t row = r0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
+  const int lane = threadIdx.x % VEC;
+  A s = 0;
+  if (row < r1)
+    for (int k = rp[row] + lane; k < rp[row + 1]; k += VEC) s += (A)va[k] * (A)x[ci[k]];
+  s = group_sum<VEC>(s);
+  if (row < r1 && lane == 0) tmp[row - r0] = (X)((A)x[row] + ((A)r[row] - s) / (A)d[row - r0]);
+}
+
+template <class X>
+__global__ void k_copy_range(int64_t n, const X* __restrict__ src, X* __restrict__ dst) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i];
+}
+
+template <class X>
+__global__ void k_dense_gemv(int64_t n, const X* __restrict__ M, const X* __restrict__ r, X* __restrict__ x) {
+  using A = typename Acc<X>::type;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  A s = 0;
+  if (row < n)
+    for (int64_t j = lane; j < n; j += 32) s += (A)M[row * n + j] * (A)r[j];
+  s = group_sum<32>(s);
+  if (row < n && lane == 0) x[row] = (X)s;
+}
+
+template <class X>
+__global__ void k_diag_solve(int64_t n, const int* __restrict__ rp, const X* __restrict__ va, const X* __restrict__ r,
+                             X* __restrict__ x) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = r[i] / va[rp[i]];
+}
+
+template <class A, class B>
+__global__ void k_convert(int64_t n, const A* __restrict__ in, B* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (B)in[i];
+}
+template <>
+__global__ void k_convert<double, __nv_bfloat16>(int64_t n, const double* __restrict__ in,
+                                                 __nv_bfloat16* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = __double2bfloat16(in[i]);
+}
+
+__global__ void k_gather(int64_t n, const int* __restrict__ perm, const double* __restrict__ in,
+                         double* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[perm[i]];
+}
+__global__ void k_scatter(int64_t n, const int* __restrict__ perm, const double* __restrict__ in,
+                          double* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[perm[i]] = in[i];
+}
+
+__global__ void k_axpy(int64_t n, double alpha, const double* __restrict__ x, double* __restrict__ y) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += alpha * x[i];
+}
+
+__global__ void k_strided_copy(int64_t n, const double* __restrict__ src, int64_t ss, double* __restrict__ dst,
+                               int64_t ds) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i * ds] = src[i * ss];
+}
+
+template <class X>
+__global__ void k_zero(int64_t n, X* __restrict__ x) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = (X)0;
+}
+
+// ------------------------------------------------------------ reductions
+constexpr int RED_BLOCKS = 512;
+
+__device__ unsigned int g_retire = 0;
+__device__ double g_partials[RED_BLOCKS];
+
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double ws[BLK / 32];
+  v = group_sum<32>(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) ws[w] = v;
+  __syncthreads();
+  double s = 0;
+  if (w == 0) {
+    s = lane < BLK / 32 ? ws[lane] : 0.0;
+    s = group_sum<32>(s);
+  }
+  __syncthreads();
+  return s;  // valid in thread 0
+}
+
+// Partial of this block -> g_partials; the last block sums them in order.
+__device__ __forceinline__ void finish_reduction(double partial, double* dst) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    g_partials[blockIdx.x] = partial;
+    __threadfence();
+    unsigned done = atomicInc(&g_retire, gridDim.x - 1);  // wraps to 0 for the last block
+    last = (done == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) {
+    double s = 0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += BLK) s += ((volatile double*)g_partials)[b];
+    s = block_sum(s);
+    if (threadIdx.x == 0) *dst = s;
+  }
+}
+
+__global__ void k_dot(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* dst) {
+  double s = 0;
+  for (int64_t i = (int64_t)blockIdx.x * BLK + threadIdx.x; i < n; i += (int64_t)gridDim.x * BLK) s += a[i] * b[i];
+  s = block_sum(s);
+  finish_reduction(s, dst);
+}
+
+template <int VEC>
+__global__ void k_spmv_dot(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci,
+                           const double* __restrict__ va, const double* __restrict__ p, double* __restrict__ y,
+                           double* dst) {
+  // warps stride over the rows uniformly so every lane joins each shuffle
+  constexpr int GPW = 32 / VEC;
+  const int lane = threadIdx.x % VEC, sub = (threadIdx.x & 31) / VEC;
+  const int64_t nwarps = (int64_t)gridDim.x * (BLK / 32);
+  double part = 0;
+  for (int64_t w = ((int64_t)blockIdx.x * BLK + threadIdx.x) / 32; w * GPW < m; w += nwarps) {
+    const int64_t g = w * GPW + sub;
+    double s = 0;
+    if (g < m)
+      for (int k = rp[g] + lane; k < rp[g + 1]; k += VEC) s += va[k] * p[ci[k]];
+    s = group_sum<VEC>(s);
+    if (g < m && lane == 0) {
+      y[g] = s;
+      part += s * p[g];
+    }
+  }
+  part = block_sum(part);
+  finish_reduction(part, dst);
+}
+
+__global__ void k_cg_update_xr(int64_t n, const double* __restrict__ sc, int num, int den, double* __restrict__ x,
+                               double* __restrict__ r, const double* __restrict__ p, const double* __restrict__ q,
+                               double* dst) {
+  const double alpha = sc[num] / sc[den];
+  double s = 0;
+  for (int64_t i = (int64_t)blockIdx.x * BLK + threadIdx.x; i < n; i += (int64_t)gridDim.x * BLK) {
+    x[i] += alpha * p[i];
+    const double ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    s += ri * ri;
+  }
+  s = block_sum(s);
+  finish_reduction(s, dst);
+}
+
+__global__ void k_cg_update_p(int64_t n, const double* __restrict__ sc, int num, int den, const double* __restrict__ z,
+                              double* __restrict__ p) {
+  const double beta = sc[num] / sc[den];
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = z[i] + beta * p[i];
+}
+
+// ----------------------------------------------------------- setup kernels
+__global__ void k_perm_row_len(int64_t m, const int* __restrict__ rp, const int* __restrict__ rperm,
+                               int* __restrict__ len) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) len[i] = rp[rperm[i] + 1] - rp[rperm[i]];
+}
+
+__global__ void k_perm_fill(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci,
+                            const double* __restrict__ va, const int* __restrict__ rperm, const int* __restrict__ cmap,
+                            const int* __restrict__ orp, int* __restrict__ oci, double* __restrict__ ova) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= m) return;
+  const int src = rp[rperm[row]], len = rp[rperm[row] + 1] - src, dst = orp[row];
+  for (int k = lane; k < len; k += 32) {
+    oci[dst + k] = cmap[ci[src + k]];
+    ova[dst + k] = va[src + k];
+  }
+}
+
+__global__ void k_l1_diag(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
+                          const double* __restrict__ va, double* __restrict__ d) {
+  int64_t j = r0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= r1) return;
+  double s = va[rp[j]];
+  for (int k = rp[j] + 1; k < rp[j + 1]; ++k)
+    if (ci[k] >= r0 && ci[k] < r1) s += fabs(va[k]);
+  d[j - r0] = s;
+}
+
+__global__ void k_csr_to_dense(int64_t n, const int* __restrict__ rp, const int* __restrict__ ci,
+                               const double* __restrict__ va, double* __restrict__ M) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int k = rp[i]; k < rp[i + 1]; ++k) M[i * n + ci[k]] = va[k];
+}
+
+__global__ void k_identity(int64_t n, double* __restrict__ M) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n * n) M[t] = (t / n == t % n) ? 1.0 : 0.0;
+}
+
+// pivot search and row swap/scale for column c (one block)
+__global__ void k_gj_pivot(int64_t n, int64_t c, double* __restrict__ M, double* __restrict__ I,
+                           double* __restrict__ colc, int* __restrict__ singular) {
+  __shared__ double bv[1024];
+  __shared__ int bi[1024];
+  double best = -1.0;
+  int arg = (int)c;
+  for (int64_t r = c + threadIdx.x; r < n; r += blockDim.x) {
+    double a = fabs(M[r * n + c]);
+    if (a > best) { best = a; arg = (int)r; }
+  }
+  bv[threadIdx.x] = best;
+  bi[threadIdx.x] = arg;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      double o = bv[threadIdx.x + s];
+      int oi = bi[threadIdx.x + s];
+      if (o > bv[threadIdx.x] || (o == bv[threadIdx.x] && oi < bi[threadIdx.x])) {
+        bv[threadIdx.x] = o;
+        bi[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  const int p = bi[0];
+  if (bv[0] == 0.0) {
+    if (threadIdx.x == 0) *singular = 1;
+    return;
+  }
+  if (p != c)
+    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
+      double t = M[c * n + k]; M[c * n + k] = M[p * n + k]; M[p * n + k] = t;
+      t = I[c * n + k]; I[c * n + k] = I[p * n + k]; I[p * n + k] = t;
+    }
+  __syncthreads();
+  const double d = M[c * n + c];
+  __syncthreads();
+  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
+    M[c * n + k] /= d;
+    I[c * n + k] /= d;
+  }
+  __syncthreads();
+  for (int64_t r = threadIdx.x; r < n; r += blockDim.x) colc[r] = (r == c) ? 0.0 : M[r * n + c];
+}
+
+__global__ void k_gj_eliminate(int64_t n, int64_t c, double* __restrict__ M, double* __restrict__ I,
+                               const double* __restrict__ colc, const int* __restrict__ singular) {
+  if (*singular) return;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * n * n) return;
+  const bool inv = t >= n * n;
+  const int64_t u = inv ? t - n * n : t;
+  const int64_t r = u / n, k = u % n;
+  const double f = colc[r];
+  if (f == 0.0) return;
+  double* A = inv ? I : M;
+  A[r * n + k] -= f * A[c * n + k];
+}
+
+template <class F>
+void launch_vec(int vec, F&& f) {
+  switch (vec) {
+    case 4: f(std::integral_constant<int, 4>()); break;
+    case 8: f(std::integral_constant<int, 8>()); break;
+    case 16: f(std::integral_constant<int, 16>()); break;
+    default: f(std::integral_constant<int, 32>()); break;
+  }
+}
+
+unsigned red_grid(const afp_context* ctx, int64_t n) {
+  int64_t g = (n + BLK - 1) / BLK;
+  int64_t cap = std::min<int64_t>(RED_BLOCKS, (int64_t)ctx->sm_count * 2);
+  return (unsigned)std::max<int64_t>(1, std::min(g, cap));
+}
+
+}  // namespace
+
+template <class V, class X>
+void spmv(const afp_context* ctx, const CSRView<V>& A, const X* x, X* y, bool add) {
+  launch_vec(A.vec, [&](auto VEC) {
+    constexpr int W = decltype(VEC)::value;
+    unsigned grid = grid_for(A.m * W, BLK);
+    if (add) k_spmv<W, V, X, true><<<grid, BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.cols, A.vals, x, y);
+    else k_spmv<W, V, X, false><<<grid, BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.cols, A.vals, x, y);
+  });
+  check_launch(ctx, "spmv");
+}
+
+template <class X>
+void residual(const afp_context* ctx, const CSRView<X>& A, const X* x, const X* r, X* out) {
+  launch_vec(A.vec, [&](auto VEC) {
+    constexpr int W = decltype(VEC)::value;
+    k_residual<W, X><<<grid_for(A.m * W, BLK), BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.cols, A.vals, x, r, out);
+  });
+  check_launch(ctx, "residual");
+}
+
+template <class X>
+void gs_class(const afp_context* ctx, const CSRView<X>& A, int64_t r0, int64_t r1, X* x, const X* r) {
+  if (r1 <= r0) return;
+  launch_vec(A.vec, [&](auto VEC) {
+    constexpr int W = decltype(VEC)::value;
+    k_gs_class<W, X><<<grid_for((r1 - r0) * W, BLK), BLK, 0, ctx->stream>>>(r0, r1, A.rowptr, A.cols, A.vals, x, r);
+  });
+  check_launch(ctx, "gauss-seidel class");
+}
+
+template <class X>
+void jacobi_l1_class(const afp_context* ctx, const CSRView<X>& A, int64_t r0, int64_t r1, X* x, const X* r,
+                     const X* l1diag, X* tmp) {
+  if (r1 <= r0) return;
+  launch_vec(A.vec, [&](auto VEC) {
+    constexpr int W = decltype(VEC)::value;
+    k_jacobi_l1<W, X><<<grid_for((r1 - r0) * W, BLK), BLK, 0, ctx->stream>>>(r0, r1, A.rowptr, A.cols, A.vals, x, r,
+                                                                             l1diag, tmp);
+  });
+  check_launch(ctx, "l1-jacobi class");
+  k_copy_range<X><<<grid_for(r1 - r0, BLK), BLK, 0, ctx->stream>>>(r1 - r0, tmp, x + r0);
+  check_launch(ctx, "l1-jacobi copy");
+}
+
+template <class X>
+void dense_gemv(const afp_context* ctx, int64_t n, const X* Ainv, const X* r, X* x) {
+  k_dense_gemv<X><<<grid_for(n * 32, BLK), BLK, 0, ctx->stream>>>(n, Ainv, r, x);
+  check_launch(ctx, "dense gemv");
+}
+
+template <class X>
+void diag_solve(const afp_context* ctx, const CSRView<X>& A, const X* r, X* x) {
+  k_diag_solve<X><<<grid_for(A.m, BLK), BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.vals, r, x);
+  check_launch(ctx, "diagonal solve");
+}
+
+template <class A, class B>
+void convert(const afp_context* ctx, int64_t n, const A* in, B* out) {
+  k_convert<A, B><<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, in, out);
+  check_launch(ctx, "convert");
+}
+
+void permute_gather(const afp_context* ctx, int64_t n, const int* perm, const double* in, double* out) {
+  k_gather<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, perm, in, out);
+  check_launch(ctx, "permute gather");
+}
+
+void permute_scatter(const afp_context* ctx, int64_t n, const int* perm, const double* in, double* out) {
+  k_scatter<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, perm, in, out);
+  check_launch(ctx, "permute scatter");
+}
+
+void axpy(const afp_context* ctx, int64_t n, double alpha, const double* x, double* y) {
+  k_axpy<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, alpha, x, y);
+  check_launch(ctx, "axpy");
+}
+
+void strided_copy(const afp_context* ctx, int64_t n, const double* src, int64_t ss, double* dst, int64_t ds) {
+  k_strided_copy<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, src, ss, dst, ds);
+  check_launch(ctx, "strided copy");
+}
+
+template <class X>
+void fill_zero(const afp_context* ctx, int64_t n, X* x) {
+  k_zero<X><<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, x);
+  check_launch(ctx, "zero");
+}
+
+void dot(const afp_context* ctx, int64_t n, const double* a, const double* b, double* dst) {
+  k_dot<<<red_grid(ctx, n), BLK, 0, ctx->stream>>>(n, a, b, dst);
+  check_launch(ctx, "dot");
+}
+
+void spmv_dot(const afp_context* ctx, const CSRView<double>& A, const double* p, double* y, double* dst) {
+  launch_vec(A.vec, [&](auto VEC) {
+    constexpr int W = decltype(VEC)::value;
+    k_spmv_dot<W><<<red_grid(ctx, A.m * W), BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.cols, A.vals, p, y, dst);
+  });
+  check_launch(ctx, "spmv+dot");
+}
+
+void cg_update_xr(const afp_context* ctx, int64_t n, const double* s, int num, int den, double* x, double* r,
+                  const double* p, const double* q, double* dst) {
+  k_cg_update_xr<<<red_grid(ctx, n), BLK, 0, ctx->stream>>>(n, s, num, den, x, r, p, q, dst);
+  check_launch(ctx, "cg update x r");
+}
+
+void cg_update_p(const afp_context* ctx, int64_t n, const double* s, int num, int den, const double* z, double* p) {
+  k_cg_update_p<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, s, num, den, z, p);
+  check_launch(ctx, "cg update p");
+}
+
+void permute_csr(const afp_context* ctx, int64_t m, const int* rowptr, const int* cols, const double* vals,
+                 const int* rperm, const int* cmap, int64_t nnz, DevBuf<int>& orp, DevBuf<int>& oci,
+                 DevBuf<double>& ova) {
+  DevBuf<int> len(ctx, m);
+  k_perm_row_len<<<grid_for(m, BLK), BLK, 0, ctx->stream>>>(m, rowptr, rperm, len.get());
+  check_launch(ctx, "permute row lengths");
+  orp.alloc(ctx, m + 1);
+  int64_t total = exclusive_scan(ctx, len.get(), orp.get(), m);
+  AFP_REQUIRE(total == nnz, AFP_ERR_CUDA, "permutation lost entries");
+  oci.alloc(ctx, nnz);
+  ova.alloc(ctx, nnz);
+  k_perm_fill<<<grid_for(m * 32, BLK), BLK, 0, ctx->stream>>>(m, rowptr, cols, vals, rperm, cmap, orp.get(),
+                                                              oci.get(), ova.get());
+  check_launch(ctx, "permute fill");
+}
+
+void l1_diag(const afp_context* ctx, const CSRView<double>& A, int64_t r0, int64_t r1, double* d) {
+  if (r1 <= r0) return;
+  k_l1_diag<<<grid_for(r1 - r0, BLK), BLK, 0, ctx->stream>>>(r0, r1, A.rowptr, A.cols, A.vals, d);
+  check_launch(ctx, "l1 diagonal");
+}
+
+bool dense_inverse(const afp_context* ctx, const CSRView<double>& A, double* inv) {
+  const int64_t n = A.m;
+  DevBuf<double> M(ctx, n * n), colc(ctx, n);
+  DevBuf<int> singular(ctx, 1);
+  singular.zero();
+  M.zero();
+  k_csr_to_dense<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, A.rowptr, A.cols, A.vals, M.get());
+  check_launch(ctx, "dense copy");
+  k_identity<<<grid_for(n * n, BLK), BLK, 0, ctx->stream>>>(n, inv);
+  check_launch(ctx, "identity");
+  for (int64_t c = 0; c < n; ++c) {
+    k_gj_pivot<<<1, 1024, 0, ctx->stream>>>(n, c, M.get(), inv, colc.get(), singular.get());
+    check_launch(ctx, "gauss-jordan pivot");
+    k_gj_eliminate<<<grid_for(2 * n * n, BLK), BLK, 0, ctx->stream>>>(n, c, M.get(), inv, colc.get(), singular.get());
+    check_launch(ctx, "gauss-jordan eliminate");
+  }
+  int hs = 0;
+  singular.download(&hs, 1);
+  sync(ctx);
+  return hs == 0;
+}
+
+void csr_spmv(const afp_context* ctx, int64_t m, const int* rowptr, const int* cols, const double* vals,
+              const double* x, double* y) {
+  CSRView<double> A{m, rowptr, cols, vals, 8};
+  spmv<double, double>(ctx, A, x, y, false);
+}
+
+// explicit instantiations
+template void spmv<double, double>(const afp_context*, const CSRView<double>&, const double*, double*, bool);
+template void spmv<float, float>(const afp_context*, const CSRView<float>&, const float*, float*, bool);
+template void spmv<__nv_bfloat16, float>(const afp_context*, const CSRView<__nv_bfloat16>&, const float*, float*,
+                                         bool);
+template void residual<double>(const afp_context*, const CSRView<double>&, const double*, const double*, double*);
+template void residual<float>(const afp_context*, const CSRView<float>&, const float*, const float*, float*);
+template void gs_class<double>(const afp_context*, const CSRView<double>&, int64_t, int64_t, double*, const double*);
+template void gs_class<float>(const afp_context*, const CSRView<float>&, int64_t, int64_t, float*, const float*);
+template void jacobi_l1_class<double>(const afp_context*, const CSRView<double>&, int64_t, int64_t, double*,
+                                      const double*, const double*, double*);
+template void jacobi_l1_class<float>(const afp_context*, const CSRView<float>&, int64_t, int64_t, float*,
+                                     const float*, const float*, float*);
+template void dense_gemv<double>(const afp_context*, int64_t, const double*, const double*, double*);
+template void dense_gemv<float>(const afp_context*, int64_t, const float*, const float*, float*);
+template void diag_solve<double>(const afp_context*, const CSRView<double>&, const double*, double*);
+template void diag_solve<float>(const afp_context*, const CSRView<float>&, const float*, float*);
+template void convert<double, float>(const afp_context*, int64_t, const double*, float*);
+template void convert<float, double>(const afp_context*, int64_t, const float*, double*);
+template void convert<double, __nv_bfloat16>(const afp_context*, int64_t, const double*, __nv_bfloat16*);
+template void fill_zero<double>(const afp_context*, int64_t, double*);
+template void fill_zero<float>(const afp_context*, int64_t, float*);
+
+}  // namespace afp

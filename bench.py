@@ -1,0 +1,276 @@
+#!/usr/bin/env python3
+"""Benchmark of the elliptic-solve path on one GB300.
+
+Workload (default): 3D Poisson, P1 on a 64^3 Kuhn-split unit cube
+(1,572,864 tetrahedra, 274,625 DOFs), jitter 0.15h seed 1, f = sum of 8
+Gaussians, zero Dirichlet data, b = M f.  Seeded synthetic input; no public
+data set is involved.
+
+A step is one solve request against the device-resident operator and AMG
+hierarchy: CG preconditioned by one V-cycle per iteration until
+||b - A x||_2 <= tol ||b||_2, from x = 0.  `value` is mixed-precision solves/s
+(FP32 V-cycle with BF16 P/P^T, FP64 CG recurrences) at tol 1e-10, whose
+error against the FP64 reference solution is reported; the plain FP64 GPU
+drop-in's solves/s is reported beside it.  Assembly, Dirichlet elimination
+and AMG setup are timed once and reported (`setup`), as are the whole
+request latencies.  L2 is flushed (a 512 MB write) before every timed step.
+
+    python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Poisson solves/s, p50/p99 latency @1e-8 rel err: mixed-prec served vs FP64 GPU"
+WORKLOADS = {
+    "poisson3d_p1_64": lambda W: W.poisson3d_p1(64),
+    "poisson3d_p1_32": lambda W: W.poisson3d_p1(32),
+    "poisson2d_p1_256": lambda W: W.poisson2d_p1(256),
+    "elliptic2d_p2_512": lambda W: W.elliptic2d_p2(512),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="poisson3d_p1_64", choices=sorted(WORKLOADS))
+    ap.add_argument("--tol", type=float, default=1e-10)
+    return ap.parse_args()
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9 or p[0] != os.environ.get("BENCH_GPU_INDEX", p[0]):
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def vcycle_bytes(amg, vx: int, vp: int, vv: int) -> float:
+    """Algorithmic HBM bytes of one V-cycle: every smoothed level reads its
+    matrix (2s+1) times (2s Gauss-Seidel sweeps and one residual), P and P^T
+    once each, and its vectors; the dense tail inverse once."""
+    s = amg.smoothStep()
+    total = 0.0
+    nl = amg.solve_levels()
+    for l in range(nl - 1):
+        n, nnz, _ = amg.level_info(l)
+        n1 = amg.level_info(l + 1)[0]
+        pnnz = amg.projection(l)[1].shape[0]
+        total += (2 * s + 1) * (nnz * (vx + 4) + 4 * (n + 1)) + 2 * s * 3 * n * vv + 2 * n * vv
+        total += 2 * (pnnz * (vp + 4)) + 4 * (n1 + 1) + 4 * (n + 1) + 3 * n * vv + 2 * n1 * vv
+    nt = amg.level_info(nl - 1)[0]
+    total += nt * nt * vv
+    return total
+
+
+def run_ours(args):
+    import torch
+    from afepack_gb300 import build as B
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import FP64, MIXED, AMGSolver
+    from afepack_gb300.fem import BoundaryConditionAdmin, Context, Space, assemble
+
+    B.build()
+    torch.cuda.init()
+    dev = torch.device("cuda:0")
+    ctx = Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    wl = WORKLOADS[args.workload](W)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    # ---- setup (timed once): assembly, b = M f, Dirichlet, AMG
+    setup = {}
+    e = [ev() for _ in range(6)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e[0].record(stream)
+    space = Space(ctx, wl.space)
+    K, M = assemble(space, wl.acc_stiff, wl.acc_mass, wl.coef)
+    e[1].record(stream)
+    f_dev = torch.from_numpy(np.ascontiguousarray(wl.f)).to(dev)
+    torch.cuda.synchronize()
+    b = M.vmult(f_dev)
+    bca = BoundaryConditionAdmin(wl.space)
+    bca.add(1, 0.0)
+    bca.apply(K, b)
+    e[2].record(stream)
+    t1 = time.perf_counter()
+    amg64 = AMGSolver(K, precision=FP64)
+    e[3].record(stream)
+    t2 = time.perf_counter()
+    amg32 = AMGSolver(K, precision=MIXED)
+    e[4].record(stream)
+    t3 = time.perf_counter()
+    torch.cuda.synchronize()
+    setup["assembly_ms"] = e[0].elapsed_time(e[1])
+    setup["rhs_dirichlet_ms"] = e[1].elapsed_time(e[2])
+    setup["amg_setup_fp64_ms"] = (t2 - t1) * 1e3
+    setup["amg_setup_mixed_ms"] = (t3 - t2) * 1e3
+    setup["assembly_wall_ms"] = (t1 - t0) * 1e3
+    levels = [amg64.level_info(l) for l in range(amg64.solve_levels())]
+
+    # ---- FP64 reference solution (tight) for the error of the timed solves
+    x_ref, info_ref = amg64.pcg(b, 1e-14, 1000)
+    torch.cuda.synchronize()
+
+    def solve(amg, tol):
+        x = torch.zeros_like(b)
+        return x, amg.pcg(b, tol, 1000, x)[1]
+
+    results = {}
+    clocks = Clocks()
+    for name, amg in (("fp64", amg64), ("mixed", amg32)):
+        for _ in range(max(args.warmup, 3)):
+            solve(amg, args.tol)
+        times, iters = [], []
+        if name == "mixed":
+            clocks.start()
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            s0, s1 = ev(), ev()
+            s0.record(stream)
+            x, info = solve(amg, args.tol)
+            s1.record(stream)
+            torch.cuda.synchronize()
+            times.append(s0.elapsed_time(s1))
+            iters.append(info["iterations"])
+        if name == "mixed":
+            clk = clocks.stop()
+        err = float(torch.linalg.norm(x - x_ref) / torch.linalg.norm(x_ref))
+        t = np.array(times)
+        results[name] = {"solves_per_s": 1e3 * len(t) / t.sum(), "ms_mean": float(t.mean()),
+                         "p50_ms": float(np.percentile(t, 50)), "p99_ms": float(np.percentile(t, 99)),
+                         "pcg_iterations": int(np.median(iters)), "rel_err_vs_fp64": err}
+
+    # ---- end to end through the C ABI with host buffers (H2D of b, D2H of x inside)
+    b_host = b.cpu().numpy().copy()
+    bh = torch.from_numpy(b_host).pin_memory()
+    xh = torch.zeros(bh.shape[0], dtype=torch.float64).pin_memory()
+    e2e_t = []
+    for i in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        xh.zero_()
+        s0, s1 = ev(), ev()
+        s0.record(stream)
+        amg32.pcg(bh.numpy(), args.tol, 1000, xh.numpy())
+        s1.record(stream)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_t.append(s0.elapsed_time(s1))
+    e2e_t = np.array(e2e_t)
+
+    # ---- roofline of the V-cycle (mixed): bytes per V-cycle / time per V-cycle
+    vb = vcycle_bytes(amg32, 4, 2, 4)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    n0, nnz0, _ = levels[0]
+    it = results["mixed"]["pcg_iterations"]
+    # per iteration: one V-cycle + FP64 SpMV + ~10 vector passes
+    iter_bytes = vb + nnz0 * 12 + 4 * (n0 + 1) + 2 * n0 * 8 + 10 * n0 * 8
+    achieved = it * iter_bytes / (results["mixed"]["ms_mean"] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "PCG iteration (V-cycle + SpMV + vector ops), mixed",
+            "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+            "traffic": None, "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"}
+
+    launches = ctx.launch_count()
+    line = {
+        "metric": METRIC, "value": round(results["mixed"]["solves_per_s"], 3), "unit": "solves/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(results["mixed"]["ms_mean"], 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 V-cycle (bf16 P/P^T) + fp64 CG", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "n_dof": int(n0), "nnz": int(nnz0), "tol": args.tol,
+                   "levels": [list(map(int, l)) for l in levels], "l2": "flushed before every step (512 MB write)",
+                   "parallelism": "replicas only"},
+        "p50_ms": round(results["mixed"]["p50_ms"], 3), "p99_ms": round(results["mixed"]["p99_ms"], 3),
+        "rel_err_vs_fp64": results["mixed"]["rel_err_vs_fp64"], "fp64": results["fp64"],
+        "mixed_over_fp64": round(results["mixed"]["solves_per_s"] / results["fp64"]["solves_per_s"], 3),
+        "setup": {k: round(v, 3) for k, v in setup.items()},
+        "e2e": {"value": round(1e3 * len(e2e_t) / e2e_t.sum(), 3), "unit": "solves/s",
+                "h2d_bytes_per_step": int(bh.numel() * 8), "d2h_bytes_per_step": int(xh.numel() * 8),
+                "p50_ms": round(float(np.percentile(e2e_t, 50)), 3), "p99_ms": round(float(np.percentile(e2e_t, 99)), 3)},
+        "roofline": roof, "clocks": clk, "gpu_launches": int(launches),
+    }
+    return line
+
+
+def run_reference(args):
+    return {"impl": "reference", "unavailable": "reference arm not wired yet"}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    line = run_ours(args)
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,204 @@
+/*
+ * afepack_gb300 -- C ABI of a GB300-native (sm_103a) implementation of
+ * AFEPack's elliptic-solve path: P1/P2 stiffness/mass assembly into AFEPack's
+ * CSR sparsity pattern, Dirichlet elimination, the classical C/F AMG
+ * hierarchy with a GPU Galerkin product, the V-cycle with a multicolour
+ * Gauss-Seidel smoother, and an outer preconditioned CG.
+ *
+ * Every entry point returns an afp_status; afp_last_error() gives the message
+ * of the calling thread's last failure.  Objects are opaque handles owning
+ * device memory.  Unless stated otherwise a double / int32 array argument may
+ * live in host memory or in device memory of the context's GPU (copies go
+ * through unified addressing); all work is ordered on the context's stream and
+ * every call returns only after its results are visible to the caller.
+ *
+ * Matrices use AFEPack's SparsityPattern convention
+ * (include/AFEPack/SparsityPattern.h:76-126,193-237): for a square matrix the
+ * diagonal entry is the first of its row and the remaining column numbers are
+ * ascending.  Row starts and column numbers are 32-bit here (AFEPack uses
+ * size_t); afp_matrix_download widens nothing, callers widen if they need to.
+ *
+ * Reference interfaces each group replaces are cited beside it (paths within
+ * the AFEPack source tree).
+ */
+#ifndef AFEPACK_GB300_H
+#define AFEPACK_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AFP_VERSION 1
+
+typedef enum afp_status {
+  AFP_OK = 0,
+  AFP_ERR_INVALID = 1,        /* bad argument (null handle, size, option)      */
+  AFP_ERR_CUDA = 2,           /* CUDA runtime failure                          */
+  AFP_ERR_NO_DEVICE = 3,      /* no usable sm_103 GPU                          */
+  AFP_ERR_OUT_OF_MEMORY = 4,  /* device or host allocation failed              */
+  AFP_ERR_NOT_CONVERGED = 5,  /* iteration limit reached above the tolerance   */
+  AFP_ERR_BREAKDOWN = 6,      /* NaN/Inf or a zero denominator in a recurrence */
+  AFP_ERR_SINGULAR = 7,       /* singular coarsest matrix                      */
+  AFP_ERR_TIMEOUT = 8,        /* a bounded wait ran out                        */
+  AFP_ERR_UNSUPPORTED = 9,    /* input outside what the kernels handle         */
+  AFP_ERR_CAPACITY = 10       /* request cannot be admitted (memory/slots)     */
+} afp_status;
+
+typedef struct afp_context afp_context;
+typedef struct afp_space afp_space;
+typedef struct afp_matrix afp_matrix;
+typedef struct afp_amg afp_amg;
+
+/* ---------------------------------------------------------------- misc */
+int afp_version(void);
+const char *afp_status_string(afp_status s);
+const char *afp_last_error(void);
+
+/* ------------------------------------------------------------- context */
+/* A context binds one GPU and one CUDA stream (a new non-blocking stream). */
+afp_status afp_context_create(int device, afp_context **out);
+afp_status afp_context_destroy(afp_context *ctx);
+afp_status afp_context_synchronize(afp_context *ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or timing events with the library's. */
+afp_status afp_context_stream(const afp_context *ctx, void **stream);
+/* Number of this library's kernel launches issued on the context so far. */
+afp_status afp_context_launch_count(const afp_context *ctx, int64_t *count);
+
+/* --------------------------------------------------------------- space */
+/* Mesh and DOF map of a Lagrange P1/P2 space on triangles (dim 2) or
+ * tetrahedra (dim 3): the data AFEPack's FEMSpace holds after
+ * buildElement/buildDof (include/AFEPack/FEMSpace.templates.h:884-1003).
+ * coords [n_vertex*dim]; cells [n_cell*(dim+1)] positively oriented vertex
+ * lists; elem_dof [n_cell*nd] global DOF of each template DOF (nd = 3,6 in
+ * 2D, 4,10 in 3D, template order of triangle.{1,2}.tmp_dof /
+ * tetrahedron.{1,2}.tmp_dof). */
+afp_status afp_space_create(afp_context *ctx, int dim, int degree, int64_t n_vertex,
+                            const double *coords, int64_t n_cell, const int32_t *cells,
+                            int64_t n_dof, const int32_t *elem_dof, afp_space **out);
+afp_status afp_space_destroy(afp_space *sp);
+
+/* ------------------------------------------------------------ assembly */
+typedef struct afp_assemble_opts {
+  int acc_stiff;        /* algebraic accuracy of the stiffness quadrature  */
+  int acc_mass;         /* algebraic accuracy of the mass quadrature       */
+  const double *coef;   /* per-cell coefficient a_e of -div(a grad u), or NULL */
+} afp_assemble_opts;
+
+/* StiffMatrix<DIM,double>::build and MassMatrix<DIM,double>::build
+ * (include/AFEPack/BilinearOperator.templates.h:56-255, element matrices of
+ * :343-406): builds the sparsity pattern once and fills the stiffness matrix
+ * (scaled per cell by coef when given) and, if mass != NULL, the mass matrix
+ * in the same pattern. */
+afp_status afp_assemble(afp_space *sp, const afp_assemble_opts *opts, afp_matrix **stiff,
+                        afp_matrix **mass);
+
+/* ------------------------------------------------------------- matrices */
+/* A device copy of a CSR matrix given in AFEPack's layout. */
+afp_status afp_matrix_create_csr(afp_context *ctx, int64_t m, int64_t n, int64_t nnz,
+                                 const int32_t *rowptr, const int32_t *cols, const double *vals,
+                                 afp_matrix **out);
+afp_status afp_matrix_info(const afp_matrix *a, int64_t *m, int64_t *n, int64_t *nnz);
+/* Copies the pattern and values out (any argument may be NULL to skip). */
+afp_status afp_matrix_download(const afp_matrix *a, int32_t *rowptr, int32_t *cols, double *vals);
+/* y = A x  (SparseMatrix::vmult, include/AFEPack/SparseMatrix.h:100-114) */
+afp_status afp_matrix_vmult(afp_matrix *a, const double *x, double *y);
+afp_status afp_matrix_destroy(afp_matrix *a);
+
+/* BoundaryConditionAdmin::apply(A, u, f, preserve_symmetry)
+ * (include/AFEPack/FEMSpace.templates.h:1338-1366): for every DOF i with
+ * dirichlet[i] != 0, f_i = a_ii g_i and row i's off-diagonal entries become 0;
+ * with preserve_symmetry the column entries a_ki become 0 too after
+ * f_k -= a_ki f_i / a_ii.  The pattern is kept.  g == NULL means zero data. */
+afp_status afp_apply_dirichlet(afp_matrix *a, double *f, const int32_t *dirichlet,
+                               const double *g, int preserve_symmetry);
+
+/* ------------------------------------------------------------------ AMG */
+typedef enum afp_precision {
+  AFP_PRECISION_FP64 = 0,   /* V-cycle in FP64                                   */
+  AFP_PRECISION_MIXED = 1   /* V-cycle in FP32 (BF16 P/P^T), FP64 outer recurrences */
+} afp_precision;
+
+typedef struct afp_amg_opts {
+  double tolerance;     /* AMGSolver toler (default 1e-12)                      */
+  int smooth_step;      /* Gauss-Seidel sweeps per smoothing (default 3)        */
+  int max_coarse;       /* n_most_project_order (default 50)                    */
+  double min_density;   /* n_most_project_sparse_degree (default 0.382)         */
+  double alpha;         /* strong-connection threshold (default 0.25)           */
+  int precision;        /* afp_precision of the V-cycle (default FP64)          */
+  int dense_tail;       /* levels with at most this many rows are solved with a
+                           dense inverse instead of smoothed (default 1024;
+                           0 keeps the reference depth)                         */
+  int max_colors;       /* colour classes of the smoother before rows fall into
+                           an l1-Jacobi overflow class (default 32)             */
+  int symmetric;        /* post-smoothing visits colours in reverse order so the
+                           V-cycle is a symmetric preconditioner (default 1)    */
+} afp_amg_opts;
+
+typedef struct afp_solve_info {
+  int iterations;       /* V-cycles (stationary solve) or CG iterations        */
+  int converged;        /* 1 when the stopping test was met                    */
+  double initial_residual;
+  double final_residual;   /* l1 norm (stationary) or relative l2 (PCG)        */
+  double seconds;          /* device time of the call                          */
+} afp_solve_info;
+
+void afp_amg_default_opts(afp_amg_opts *opts);
+
+/* AMGSolver::reinit (src/AMGSolver.cpp:384-438): the C/F splitting of
+ * Project (:18-226) runs on the host, the Galerkin product P A P^T of
+ * getPMPt (:288-358) on the GPU, level by level, until the reference's stop
+ * rule (order <= max_coarse and density >= min_density) holds. */
+afp_status afp_amg_setup(afp_matrix *a, const afp_amg_opts *opts, afp_amg **out);
+afp_status afp_amg_destroy(afp_amg *amg);
+afp_status afp_amg_num_levels(const afp_amg *amg, int *n_project, int *solve_levels);
+/* level l (0 = fine): order, stored entries, smoother colour classes
+ * (-1 for the dense tail level) */
+afp_status afp_amg_level_info(const afp_amg *amg, int level, int64_t *n, int64_t *nnz, int *colors);
+/* Downloads level l's Galerkin matrix (l >= 1) or projection P_l (l >= 0) in
+ * the reference's orientation (P is n_{l+1} x n_l) and the reference's row
+ * order; pass NULL to skip an array. */
+afp_status afp_amg_download_level(const afp_amg *amg, int level, int32_t *rowptr, int32_t *cols,
+                                  double *vals);
+afp_status afp_amg_download_projection(const afp_amg *amg, int level, int32_t *rowptr,
+                                       int32_t *cols, double *vals);
+
+/* AMGSolver::solve(x, r, tol, step, mode) (src/AMGSolver.cpp:549-639):
+ * step+1 V-cycles starting from x; tol only decides `converged`
+ * (l1 residual < tol * initial l1 residual; tol == 0 uses the solver's). */
+afp_status afp_amg_solve(afp_amg *amg, double *x, const double *r, double tol, int64_t step,
+                         int mode, afp_solve_info *info);
+/* AMGPreconditioner::vmult(x, b) (include/AFEPack/AMGSolver.h:193-195):
+ * iterate_step+1 V-cycles from the given x. */
+afp_status afp_amg_precondition(afp_amg *amg, double *x, const double *b, int iterate_step);
+
+/* Conjugate gradients preconditioned by one V-cycle per iteration, the
+ * solver shape of examples/FAST/src/poisson_solver_comparison_afepack.cpp:197-253
+ * (which the library itself does not provide): stops when
+ * ||b - A x||_2 <= tol ||b||_2.  x holds the initial guess on entry.
+ * With a mixed-precision hierarchy the V-cycle runs in FP32 and the CG
+ * recurrences, residuals and dot products in FP64. */
+afp_status afp_pcg_solve(afp_amg *amg, double *x, const double *b, double tol, int maxit,
+                         afp_solve_info *info);
+/* nrhs systems with the same matrix; X and B are n x nrhs row-major.  One
+ * batched launch per kernel serves all right-hand sides; every column has
+ * its own CG recurrences and stopping test. info may be NULL or nrhs long. */
+afp_status afp_pcg_solve_multi(afp_amg *amg, double *X, const double *B, int nrhs, double tol,
+                               int maxit, afp_solve_info *info);
+
+/* ----------------------------------------------------------- host logic */
+/* The C/F splitting and projection of one level (Project, src/AMGSolver.cpp:18-226),
+ * run on the host on a host CSR; no GPU needed.  cf receives -1 for C and 1
+ * for F points.  P (n_coarse x m, sorted columns) is returned through
+ * buffers the library allocates; release them with afp_host_free. */
+afp_status afp_host_coarsen(int64_t m, const int32_t *rowptr, const int32_t *cols,
+                            const double *vals, double alpha, int32_t *cf, int64_t *n_coarse,
+                            int32_t **p_rowptr, int32_t **p_cols, double **p_vals);
+void afp_host_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AFEPACK_GB300_H */

@@ -1,0 +1,151 @@
+"""GPU AMG: hierarchy parity with the reference, V-cycle and PCG solutions
+against the oracle and an FP64 direct solve, mixed precision accuracy."""
+import numpy as np
+import pytest
+import scipy.sparse as sps
+import scipy.sparse.linalg as spla
+
+import oracle as O
+from conftest import golden_csr, golden_names, golden_space, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def system(ctx, wl):
+    from afepack_gb300.fem import BoundaryConditionAdmin, Space, assemble
+    space = Space(ctx, wl.space)
+    K, M = assemble(space, wl.acc_stiff, wl.acc_mass, wl.coef)
+    b = M.vmult(wl.f)
+    bca = BoundaryConditionAdmin(wl.space)
+    bca.add(1, 0.0)
+    bca.apply(K, b)
+    return space, K, b
+
+
+def direct(K, b):
+    rp, ci, va = K.download()
+    A = sps.csr_matrix((va, ci, rp), shape=(rp.shape[0] - 1,) * 2).tocsc()
+    return spla.splu(A).solve(b)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_hierarchy_matches_reference(ctx, name):
+    from afepack_gb300.amg import AMGSolver
+    from afepack_gb300.fem import SparseMatrix
+    g = load_golden(name)
+    S = golden_csr(g, "system")
+    K = SparseMatrix.from_csr(ctx, S.rowptr, S.cols, S.vals)
+    amg = AMGSolver(K, dense_tail=0)
+    assert amg.n_project() == int(g["n_project"])
+    for l in range(amg.n_project()):
+        P, A = golden_csr(g, f"P{l}"), golden_csr(g, f"A{l + 1}")
+        prp, pci, pva = amg.projection(l)
+        arp, aci, ava = amg.level_matrix(l + 1)
+        assert np.array_equal(prp, P.rowptr) and np.array_equal(pci, P.cols) and np.array_equal(pva, P.vals)
+        assert np.array_equal(arp, A.rowptr) and np.array_equal(aci, A.cols) and np.array_equal(ava, A.vals)
+
+
+def test_hierarchy_matches_oracle_poisson2d(ctx):
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import AMGSolver
+    wl = W.poisson2d_p1(128)
+    _, K, b = system(ctx, wl)
+    amg = AMGSolver(K, dense_tail=0)
+    rp, ci, va = K.download()
+    ho = O.AMG(O.CSR(rp, ci, va, (rp.shape[0] - 1,) * 2))
+    assert amg.n_project() == ho.n_level
+    for l in range(ho.n_level):
+        A = ho.level(l + 1)
+        arp, aci, ava = amg.level_matrix(l + 1)
+        assert np.array_equal(arp, A.rowptr) and np.array_equal(aci, A.cols) and np.array_equal(ava, A.vals)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_vcycles_converge(ctx, name):
+    from afepack_gb300.amg import AMGSolver
+    from afepack_gb300.fem import SparseMatrix
+    g = load_golden(name)
+    S = golden_csr(g, "system")
+    K = SparseMatrix.from_csr(ctx, S.rowptr, S.cols, S.vals)
+    for tail in (0, 1024):
+        amg = AMGSolver(K, dense_tail=tail)
+        x = np.zeros_like(g["rhs"])
+        info = amg.solve(x, g["rhs"], 0.0, 29)
+        assert info["iterations"] == 30
+        assert info["final_residual"] < 1e-8 * info["initial_residual"]
+        xd = spla.splu(S.to_scipy().tocsc()).solve(g["rhs"])
+        assert np.abs(x - xd).max() <= 1e-7 * np.abs(xd).max()
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_pcg_matches_reference_solution(ctx, name):
+    from afepack_gb300.amg import AMGSolver
+    from afepack_gb300.fem import SparseMatrix
+    g = load_golden(name)
+    S = golden_csr(g, "system")
+    K = SparseMatrix.from_csr(ctx, S.rowptr, S.cols, S.vals)
+    amg = AMGSolver(K, dense_tail=0)
+    x, info = amg.pcg(g["rhs"], 1e-10, 200)
+    assert info["converged"] and info["final_residual"] <= 1e-10
+    ref = g["x_pcg"]
+    assert np.abs(x - ref).max() <= 1e-8 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_pcg_poisson2d_vs_direct(ctx, precision):
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import AMGSolver
+    wl = W.poisson2d_p1(256)
+    _, K, b = system(ctx, wl)
+    amg = AMGSolver(K, precision=precision)
+    x, info = amg.pcg(b, 1e-10 if precision == 0 else 1e-10, 300)
+    xd = direct(K, b)
+    err = np.linalg.norm(x - xd) / np.linalg.norm(xd)
+    assert info["converged"], info
+    assert err <= 1e-8, err
+    # the reference's own CG + V-cycle (oracle) reaches the same solution
+    rp, ci, va = K.download()
+    Ao = O.CSR(rp, ci, va, (rp.shape[0] - 1,) * 2)
+    xo, it, rel = O.AMG(Ao).pcg(b, 1e-10)
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) <= 1e-8
+
+
+def test_pcg_3d_p2_variable_coefficient(ctx):
+    from afepack_gb300.amg import AMGSolver
+    from afepack_gb300.mesh import FESpace, cube_mesh
+    from afepack_gb300.workloads import Workload
+    mesh = cube_mesh(8, 0.15, 9)
+    sp = FESpace(mesh, 2)
+    rng = np.random.default_rng(2)
+    wl = Workload("t", sp, np.exp(rng.standard_normal(mesh.n_cell)), rng.standard_normal(sp.n_dof), 4, 4)
+    _, K, b = system(ctx, wl)
+    for precision in (0, 1):
+        amg = AMGSolver(K, precision=precision)
+        x, info = amg.pcg(b, 1e-10, 300)
+        xd = direct(K, b)
+        assert info["converged"]
+        assert np.linalg.norm(x - xd) / np.linalg.norm(xd) <= 1e-8
+
+
+def test_multi_rhs_matches_single(ctx):
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import AMGSolver
+    wl = W.poisson2d_p1(64)
+    _, K, b = system(ctx, wl)
+    amg = AMGSolver(K)
+    B = np.stack([b, 2 * b, np.roll(b, 3)], axis=1)
+    X, infos = amg.pcg_multi(B, 1e-10, 300)
+    for k in range(3):
+        xk, _ = amg.pcg(np.ascontiguousarray(B[:, k]), 1e-10, 300)
+        assert np.abs(X[:, k] - xk).max() <= 1e-12 * np.abs(xk).max()
+
+
+def test_launch_counter_moves(ctx):
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import AMGSolver
+    wl = W.poisson2d_p1(32)
+    _, K, b = system(ctx, wl)
+    amg = AMGSolver(K)
+    before = ctx.launch_count()
+    amg.pcg(b, 1e-8, 100)
+    assert ctx.launch_count() > before
