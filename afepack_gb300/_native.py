@@ -64,12 +64,15 @@ SIGNATURES = {
     "afp_matrix_create_csr": [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                               c_void_pp],
     "afp_matrix_info": [C.c_void_p, c_i64p, c_i64p, c_i64p],
+    "afp_matrix_set_values": [C.c_void_p, C.c_void_p],
     "afp_matrix_download": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
     "afp_matrix_vmult": [C.c_void_p, C.c_void_p, C.c_void_p],
     "afp_matrix_destroy": [C.c_void_p],
     "afp_apply_dirichlet": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],
     "afp_amg_default_opts": [C.POINTER(AMGOpts)],
     "afp_amg_setup": [C.c_void_p, C.POINTER(AMGOpts), c_void_pp],
+    "afp_amg_setup_lazy": [C.c_void_p, C.POINTER(AMGOpts), c_void_pp],
+    "afp_amg_lazy_reinit": [C.c_void_p, C.c_void_p],
     "afp_amg_destroy": [C.c_void_p],
     "afp_amg_num_levels": [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)],
     "afp_amg_level_info": [C.c_void_p, C.c_int, c_i64p, c_i64p, C.POINTER(C.c_int)],

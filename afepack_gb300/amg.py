@@ -146,12 +146,30 @@ class AMGSolver:
         return X, [i.as_dict() for i in infos]
 
 
+    def lazyReinit(self, M: SparseMatrix):
+        """AMGSolver::lazyReinit: the lazyProject hierarchy on first use, then
+        numeric re-setup for new values on the same pattern."""
+        if self.handle is None:
+            h = C.c_void_p()
+            N.call("afp_amg_setup_lazy", M.handle, C.byref(self.opts), C.byref(h))
+            self.handle = h
+        else:
+            N.call("afp_amg_lazy_reinit", self.handle, M.handle)
+        self.matrix = M
+
+
 class AMGPreconditioner(AMGSolver):
-    """AMGPreconditioner(M, is=5, s=3): vmult(x, b) runs is+1 V-cycles from x."""
+    """AMGPreconditioner(M, is=5, s=3): lazy hierarchy; vmult(x, b) runs is+1 V-cycles from x."""
 
     def __init__(self, M: SparseMatrix | None = None, iterate_step: int = 5, s: int = 3, **kw):
         self.iterate_step = iterate_step
-        super().__init__(M, s=s, **kw)
+        super().__init__(None, s=s, **kw)
+        if M is not None:
+            self.lazyReinit(M)
+
+    def reinit(self, M: SparseMatrix, iterate_step: int = 5):
+        self.lazyReinit(M)
+        self.iterate_step = iterate_step
 
     def vmult(self, x, b):
         N.call("afp_amg_precondition", self.handle, N.ptr(x), N.ptr(b), self.iterate_step)

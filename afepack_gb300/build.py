@@ -27,9 +27,10 @@ SOURCES = [
     ("rap.cu", ["-fmad=false"]),
     ("solve.cu", []),
     ("amg.cu", []),
+    ("mrhs.cu", []),
     ("coarsen_host.cpp", []),
 ]
-HEADERS = ["common.cuh", "kernels.cuh", "solve.cuh", "quadrature_tables.h"]
+HEADERS = ["common.cuh", "kernels.cuh", "solve.cuh", "amg_internal.cuh", "quadrature_tables.h"]
 
 
 def _nvcc() -> str:

@@ -18,70 +18,9 @@
 #include <cmath>
 #include <numeric>
 
-#include "kernels.cuh"
-#include "solve.cuh"
-
-namespace afp {
-
-struct Level {
-  int64_t n = 0, nnz = 0;
-  DevBuf<int> rp, ci;
-  DevBuf<double> va;
-  DevBuf<float> va32;
-  int vec = 8;
-  std::vector<int64_t> cls;  // class boundaries (cls.size()-1 classes)
-  bool overflow = false;     // the last class is the l1-Jacobi overflow class
-  DevBuf<double> l1d;
-  DevBuf<float> l1d32;
-  // restriction P (n_{l+1} x n_l) and prolongation P^T (n_l x n_{l+1})
-  DevBuf<int> prp, pci, trp, tci;
-  DevBuf<double> pva, tva;
-  DevBuf<__nv_bfloat16> pva16, tva16;
-  int64_t pnnz = 0;
-  int pvec = 8, tvec = 8;
-  DevBuf<int> perm;  // solve order -> reference order
-  DevBuf<double> x, r, tmp;
-  DevBuf<float> x32, r32, tmp32;
-
-  template <class X>
-  CSRView<X> A() const;
-};
-
-template <>
-CSRView<double> Level::A<double>() const {
-  return {n, rp.get(), ci.get(), va.get(), vec};
-}
-template <>
-CSRView<float> Level::A<float>() const {
-  return {n, rp.get(), ci.get(), va32.get(), vec};
-}
-
-}  // namespace afp
+#include "amg_internal.cuh"
 
 using namespace afp;
-
-struct afp_amg {
-  afp_context* ctx = nullptr;
-  afp_amg_opts opts{};
-  int n_project = 0;   // levels built (projections)
-  bool most_full = true;
-  int t = 0;           // smoothed levels 0..t-1, level t is the tail
-  bool tail_dense = true;
-  std::vector<Level> lv;
-  std::vector<HostCSR> refA, refP;  // reference-order copies for download
-  DevBuf<double> tail_inv;
-  DevBuf<float> tail_inv32;
-  // solver vectors (level-0 solve order)
-  DevBuf<double> b, x, r, z, p, q, tmp;
-  DevBuf<float> r32, z32;
-  cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
-  int64_t graph64_nodes = 0, graph32_nodes = 0;
-
-  ~afp_amg() {
-    if (graph64) cudaGraphExecDestroy(graph64);
-    if (graph32) cudaGraphExecDestroy(graph32);
-  }
-};
 
 namespace afp {
 namespace {
@@ -416,8 +355,10 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
   sync(ctx);
 }
 
-void setup(afp_amg* h, afp_matrix* A) {
+void setup(afp_amg* h, afp_matrix* A, bool lazy) {
   afp_context* ctx = h->ctx;
+  h->lazy = lazy;
+  h->pat0 = A->pat;
   const afp_amg_opts& o = h->opts;
   AFP_REQUIRE(A->pat->m == A->pat->n, AFP_ERR_INVALID, "matrix is not square");
   HostCSR H0;
@@ -434,7 +375,8 @@ void setup(afp_amg* h, afp_matrix* A) {
     const HostCSR& M = h->refA[l];
     std::vector<int> cf;
     HostCSR P, Pt;
-    host_project(M, o.alpha, cf, P, Pt);
+    if (lazy) host_lazy_project(M, P, Pt);
+    else host_project(M, o.alpha, cf, P, Pt);
     DevCSR dP, dT;
     upload_host_csr(ctx, P, dP);
     upload_host_csr(ctx, Pt, dT);
@@ -462,6 +404,7 @@ void setup(afp_amg* h, afp_matrix* A) {
     dc.va = std::move(cvals);
     refDev.push_back(std::move(dc));
     h->refP.push_back(std::move(P));
+    if (lazy) h->refPt.push_back(std::move(Pt));
     sparse_degree = (float)C.nnz() / ((float)m * m);
     h->refA.push_back(std::move(C));
     ++l;
@@ -469,6 +412,49 @@ void setup(afp_amg* h, afp_matrix* A) {
   h->n_project = l;
   h->t = l;
   h->tail_dense = h->most_full;
+  build_solve_layout(h, refDev, A);
+}
+
+// AMGSolver::lazyReinit on an initialised solver (src/AMGSolver.cpp:505-545):
+// same projections, new matrix values -- every Galerkin level is recomputed
+// on the GPU from the stored P and P^T; no host C/F work.
+void lazy_reinit(afp_amg* h, afp_matrix* A) {
+  afp_context* ctx = h->ctx;
+  AFP_REQUIRE(h->lazy, AFP_ERR_INVALID, "solver was not set up in lazy mode");
+  AFP_REQUIRE(A->pat == h->pat0, AFP_ERR_INVALID, "The solver is not initialized with the same sparsity pattern.");
+  std::vector<DevCSR> refDev(1);
+  HostCSR H0;
+  download_host_csr(ctx, A->pat->m, A->pat->n, A->pat->nnz, A->pat->rowptr.get(), A->pat->cols.get(), A->vals.get(),
+                    H0);
+  h->refA[0] = std::move(H0);
+  for (int l = 0; l < h->n_project; ++l) {
+    DevCSR dP, dT;
+    upload_host_csr(ctx, h->refP[l], dP);
+    upload_host_csr(ctx, h->refPt[l], dT);
+    const int* arp = l == 0 ? A->pat->rowptr.get() : refDev[l].rp.get();
+    const int* aci = l == 0 ? A->pat->cols.get() : refDev[l].ci.get();
+    const double* ava = l == 0 ? A->vals.get() : refDev[l].va.get();
+    Pattern cpat;
+    DevBuf<double> cvals;
+    galerkin_product(ctx, dP.m, dP.n, dP.rp.get(), dP.ci.get(), dP.va.get(), arp, aci, ava, dT.rp.get(), dT.ci.get(),
+                     dT.va.get(), cpat, cvals);
+    HostCSR C;
+    download_host_csr(ctx, cpat.m, cpat.n, cpat.nnz, cpat.rowptr.get(), cpat.cols.get(), cvals.get(), C);
+    h->refA[l + 1] = std::move(C);
+    DevCSR dc;
+    dc.m = cpat.m;
+    dc.n = cpat.n;
+    dc.nnz = cpat.nnz;
+    dc.rp = std::move(cpat.rowptr);
+    dc.ci = std::move(cpat.cols);
+    dc.va = std::move(cvals);
+    refDev.push_back(std::move(dc));
+  }
+  if (h->graph64) cudaGraphExecDestroy(h->graph64);
+  if (h->graph32) cudaGraphExecDestroy(h->graph32);
+  h->graph64 = h->graph32 = nullptr;
+  h->multi.reset();
+  h->lv.clear();
   build_solve_layout(h, refDev, A);
 }
 
@@ -575,8 +561,29 @@ afp_status afp_amg_setup(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out)
                     (o.precision == AFP_PRECISION_FP64 || o.precision == AFP_PRECISION_MIXED),
                 AFP_ERR_INVALID, "invalid AMG options");
     AFP_REQUIRE(o.dense_tail <= 8192, AFP_ERR_UNSUPPORTED, "dense_tail above 8192 rows");
-    setup(h.get(), a);
+    setup(h.get(), a, false);
     *out = h.release();
+  });
+}
+
+afp_status afp_amg_setup_lazy(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out) {
+  return guarded([&] {
+    AFP_REQUIRE(a && out, AFP_ERR_INVALID, "null argument");
+    bind(a->ctx);
+    auto h = std::make_unique<afp_amg>();
+    h->ctx = a->ctx;
+    if (opts) h->opts = *opts;
+    else afp_amg_default_opts(&h->opts);
+    setup(h.get(), a, true);
+    *out = h.release();
+  });
+}
+
+afp_status afp_amg_lazy_reinit(afp_amg* h, afp_matrix* a) {
+  return guarded([&] {
+    AFP_REQUIRE(h && a, AFP_ERR_INVALID, "null argument");
+    bind(h->ctx);
+    lazy_reinit(h, a);
   });
 }
 
@@ -690,16 +697,22 @@ afp_status afp_pcg_solve_multi(afp_amg* h, double* X, const double* B, int nrhs,
     afp_context* ctx = h->ctx;
     bind(ctx);
     const int64_t n = h->lv[0].n;
-    DevBuf<double> dB(ctx, n * nrhs), dX(ctx, n * nrhs), xc(ctx, n), bc(ctx, n);
-    dB.upload(B, n * nrhs);
-    dX.upload(X, n * nrhs);
-    for (int k = 0; k < nrhs; ++k) {
-      strided_copy(ctx, n, dB.get() + k, nrhs, bc.get(), 1);
-      strided_copy(ctx, n, dX.get() + k, nrhs, xc.get(), 1);
-      pcg(h, xc.get(), bc.get(), tol, maxit, info ? info + k : nullptr);
-      strided_copy(ctx, n, xc.get(), 1, dX.get() + k, nrhs);
+    if (nrhs <= 64) {
+      pcg_multi(h, X, B, nrhs, tol, maxit, info);
+      return;
     }
-    dX.download(X, n * nrhs);
+    // wider blocks: batches of 64 columns through contiguous staging blocks
+    DevBuf<double> bB(ctx, n * 64), bX(ctx, n * 64);
+    for (int c0 = 0; c0 < nrhs; c0 += 64) {
+      const int kc = std::min(64, nrhs - c0);
+      AFP_CUDA(cudaMemcpy2DAsync(bB.get(), kc * sizeof(double), B + c0, nrhs * sizeof(double), kc * sizeof(double), n,
+                                 cudaMemcpyDefault, ctx->stream));
+      AFP_CUDA(cudaMemcpy2DAsync(bX.get(), kc * sizeof(double), X + c0, nrhs * sizeof(double), kc * sizeof(double), n,
+                                 cudaMemcpyDefault, ctx->stream));
+      pcg_multi(h, bX.get(), bB.get(), kc, tol, maxit, info ? info + c0 : nullptr);
+      AFP_CUDA(cudaMemcpy2DAsync(X + c0, nrhs * sizeof(double), bX.get(), kc * sizeof(double), kc * sizeof(double), n,
+                                 cudaMemcpyDefault, ctx->stream));
+    }
     sync(ctx);
   });
 }

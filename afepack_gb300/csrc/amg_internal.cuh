@@ -1,0 +1,94 @@
+// Internal layout of an AMG hierarchy (shared by amg.cu and mrhs.cu).
+#pragma once
+
+#include <memory>
+
+#include "kernels.cuh"
+#include "solve.cuh"
+
+namespace afp {
+
+// One level of the solve layout (colour-permuted numbering).
+struct Level {
+  int64_t n = 0, nnz = 0;
+  DevBuf<int> rp, ci;
+  DevBuf<double> va;
+  DevBuf<float> va32;
+  int vec = 8;
+  std::vector<int64_t> cls;  // class boundaries (cls.size()-1 classes)
+  bool overflow = false;     // the last class is the l1-Jacobi overflow class
+  DevBuf<double> l1d;
+  DevBuf<float> l1d32;
+  // restriction P (n_{l+1} x n_l) and prolongation P^T (n_l x n_{l+1})
+  DevBuf<int> prp, pci, trp, tci;
+  DevBuf<double> pva, tva;
+  DevBuf<__nv_bfloat16> pva16, tva16;
+  int64_t pnnz = 0;
+  int pvec = 8, tvec = 8;
+  DevBuf<int> perm;  // solve order -> reference order
+  DevBuf<double> x, r, tmp;
+  DevBuf<float> x32, r32, tmp32;
+
+  template <class X>
+  CSRView<X> A() const;
+};
+
+template <>
+inline CSRView<double> Level::A<double>() const {
+  return {n, rp.get(), ci.get(), va.get(), vec};
+}
+template <>
+inline CSRView<float> Level::A<float>() const {
+  return {n, rp.get(), ci.get(), va32.get(), vec};
+}
+
+// Work space of the batched multi-right-hand-side solver for k columns.
+struct MultiState {
+  int k = 0;
+  bool mixed = false;
+  std::vector<DevBuf<double>> X, R, T;      // per level, n_l x k (FP64 V-cycle)
+  std::vector<DevBuf<float>> X32, R32, T32; // per level, n_l x k (FP32 V-cycle)
+  DevBuf<double> B, Xs, Rs, Z, P, Q, Tmp;   // level-0 CG blocks, n x k
+  DevBuf<double> scal;                      // column scalars, 8 x k
+  DevBuf<int> active;                       // k flags
+  cudaGraphExec_t graph = nullptr;
+  int64_t graph_nodes = 0;
+  ~MultiState() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+};
+
+}  // namespace afp
+
+struct afp_amg {
+  afp_context* ctx = nullptr;
+  afp_amg_opts opts{};
+  int n_project = 0;   // levels built (projections)
+  bool most_full = true;
+  int t = 0;           // smoothed levels 0..t-1, level t is the tail
+  bool tail_dense = true;
+  std::vector<afp::Level> lv;
+  std::vector<afp::HostCSR> refA, refP;  // reference-order copies for download
+  bool lazy = false;                      // hierarchy from lazyProject (AMGPreconditioner)
+  std::vector<afp::HostCSR> refPt;        // lazyProject's own P^T, used by the Galerkin product
+  std::shared_ptr<afp::Pattern> pat0;     // the fine matrix's pattern object (lazy re-setup check)
+  afp::DevBuf<double> tail_inv;
+  afp::DevBuf<float> tail_inv32;
+  // solver vectors (level-0 solve order)
+  afp::DevBuf<double> b, x, r, z, p, q, tmp;
+  afp::DevBuf<float> r32, z32;
+  cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
+  int64_t graph64_nodes = 0, graph32_nodes = 0;
+  std::unique_ptr<afp::MultiState> multi;
+
+  ~afp_amg() {
+    if (graph64) cudaGraphExecDestroy(graph64);
+    if (graph32) cudaGraphExecDestroy(graph32);
+  }
+};
+
+namespace afp {
+// Batched CG over nrhs columns (mrhs.cu).
+void pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, double tol, int maxit,
+               afp_solve_info* info);
+}  // namespace afp

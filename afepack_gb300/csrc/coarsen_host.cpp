@@ -196,6 +196,89 @@ void host_project(const HostCSR& M, double alpha, std::vector<int>& flag, HostCS
   }
 }
 
+// AMGSolver::lazyProject (src/AMGSolver.cpp:235-284): greedy independent set
+// of "core" rows in row order; each core row aggregates itself and its
+// neighbours, a neighbour l with weight 1/(number of core rows next to l).
+// The reference sizes both patterns with SparsityPattern::max_entries_per_row(),
+// which skips the last row (SparsityPattern.h:239-249), and
+// SparsityPattern::add silently drops entries of a full row; both are kept so
+// that P is the reference's.
+void host_lazy_project(const HostCSR& M, HostCSR& P, HostCSR& Pt) {
+  const int m = (int)M.m;
+  const int* rs = M.rowptr.data();
+  const int* cn = M.cols.data();
+  std::vector<int> counter(m, 0), core;
+  for (int i = 0; i < m; ++i) {
+    if (counter[i] > 0) continue;
+    for (int j = rs[i] + 1; j < rs[i + 1]; ++j) counter[cn[j]]++;
+    core.push_back(i);
+  }
+  const int nc = (int)core.size();
+  int cap = 0;
+  for (int i = 1; i < m; ++i) cap = std::max(cap, rs[i] - rs[i - 1]);
+  const bool square = (nc == m);
+  // slot patterns with capacity `cap` per row (diagonal preset when square)
+  std::vector<int> ps((size_t)nc * cap, -1), ts((size_t)m * cap, -1);
+  if (square && cap > 0) {
+    for (int i = 0; i < nc; ++i) ps[(size_t)i * cap] = i;
+    for (int i = 0; i < m; ++i) ts[(size_t)i * cap] = i;
+  }
+  auto add = [cap](std::vector<int>& slots, int row, int col) {
+    int* s = slots.data() + (size_t)row * cap;
+    for (int k = 0; k < cap; ++k) {
+      if (s[k] == col) return;
+      if (s[k] == -1) {
+        s[k] = col;
+        return;
+      }
+    }
+  };
+  for (int i = 0; i < nc; ++i) {
+    const int k = core[i];
+    add(ps, i, k);
+    add(ts, k, i);
+    for (int j = rs[k] + 1; j < rs[k + 1]; ++j) {
+      add(ps, i, cn[j]);
+      add(ts, cn[j], i);
+    }
+  }
+  auto compress = [cap, square](const std::vector<int>& slots, int rows, int ncols, HostCSR& out) {
+    out.m = rows;
+    out.n = ncols;
+    out.rowptr.assign(rows + 1, 0);
+    out.cols.clear();
+    for (int i = 0; i < rows; ++i) {
+      const int* s = slots.data() + (size_t)i * cap;
+      int len = 0;
+      while (len < cap && s[len] != -1) ++len;
+      const size_t b = out.cols.size();
+      out.cols.insert(out.cols.end(), s, s + len);
+      std::sort(out.cols.begin() + b + (square && len > 0 ? 1 : 0), out.cols.end());
+      out.rowptr[i + 1] = (int)out.cols.size();
+    }
+    out.vals.assign(out.cols.size(), 0.0);
+  };
+  compress(ps, nc, m, P);
+  compress(ts, m, nc, Pt);
+  auto madd = [](HostCSR& A, int i, int j, double v) {
+    for (int q = A.rowptr[i]; q < A.rowptr[i + 1]; ++q)
+      if (A.cols[q] == j) {
+        A.vals[q] += v;
+        return;
+      }
+  };
+  for (int i = 0; i < nc; ++i) {
+    const int k = core[i];
+    madd(P, i, k, 1.0);
+    madd(Pt, k, i, 1.0);
+    for (int j = rs[k] + 1; j < rs[k + 1]; ++j) {
+      const int l = cn[j];
+      madd(P, i, l, 1.0 / counter[l]);
+      madd(Pt, l, i, 1.0 / counter[l]);
+    }
+  }
+}
+
 int host_color(const HostCSR& A, int max_colors, std::vector<int>& color) {
   const int m = (int)A.m;
   color.assign(m, -1);

@@ -72,6 +72,11 @@ struct afp_context {
   // device-side scalars for reductions (lives as long as the context)
   double* d_scalars = nullptr;
   double* h_scalars = nullptr;  // pinned mirror
+  // per-context reduction scratch: block partials and the retire counter of
+  // the last-block-reduces pattern, so that contexts on different streams
+  // never share them
+  double* d_partials = nullptr;
+  unsigned* d_retire = nullptr;
 };
 
 namespace afp {

@@ -177,6 +177,9 @@ afp_status afp_context_create(int device, afp_context** out) {
     uint64_t threshold = UINT64_MAX;
     AFP_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold));
     AFP_CUDA(cudaMalloc(&ctx->d_scalars, 64 * sizeof(double)));
+    AFP_CUDA(cudaMalloc(&ctx->d_partials, 1024 * sizeof(double)));
+    AFP_CUDA(cudaMalloc(&ctx->d_retire, 16 * sizeof(unsigned)));
+    AFP_CUDA(cudaMemset(ctx->d_retire, 0, 16 * sizeof(unsigned)));
     AFP_CUDA(cudaMallocHost(&ctx->h_scalars, 64 * sizeof(double)));
     *out = ctx.release();
   });
@@ -188,6 +191,8 @@ afp_status afp_context_destroy(afp_context* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->d_scalars);
+    cudaFree(ctx->d_partials);
+    cudaFree(ctx->d_retire);
     cudaFreeHost(ctx->h_scalars);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -245,6 +250,15 @@ afp_status afp_matrix_info(const afp_matrix* a, int64_t* m, int64_t* n, int64_t*
     if (m) *m = a->pat->m;
     if (n) *n = a->pat->n;
     if (nnz) *nnz = a->pat->nnz;
+  });
+}
+
+afp_status afp_matrix_set_values(afp_matrix* a, const double* vals) {
+  return guarded([&] {
+    AFP_REQUIRE(a && vals, AFP_ERR_INVALID, "null argument");
+    bind(a->ctx);
+    a->vals.upload(vals, a->pat->nnz);
+    sync(a->ctx);
   });
 }
 

@@ -29,6 +29,9 @@ struct HostCSR {
 // its transpose; cf[i] = -1 (C) or 1 (F).
 void host_project(const HostCSR& M, double alpha, std::vector<int>& cf, HostCSR& P, HostCSR& Pt);
 
+// lazyProject(): aggregation-like projection P (n_c x m) and its transpose.
+void host_lazy_project(const HostCSR& M, HostCSR& P, HostCSR& Pt);
+
 // Greedy colouring of a square matrix's graph (nonzero off-diagonal entries
 // couple rows): colour[i] < max_colors, or max_colors for rows that found no
 // free colour (the overflow class).  Returns the number of classes used.

@@ -1,0 +1,661 @@
+// Batched multi-right-hand-side V-cycle and CG: k systems with one matrix
+// and hierarchy, all advanced by the same launches.
+//
+// Blocks are n x k row-major (the k values of one DOF are contiguous).  Every
+// row kernel gives a matrix row to one warp whose lanes own the columns: a
+// stored entry a_ij is read once and applied to all k columns of row j of the
+// block, a 128/256-byte coalesced segment.  Relative to k single solves the
+// matrix traffic drops k-fold and the arithmetic per matrix byte grows k-fold.
+//
+// CG keeps its recurrences per column: column scalars live on the device, a
+// column stops updating once its relative residual meets the tolerance, and
+// the iteration ends when every column has.
+#include <cmath>
+
+#include "amg_internal.cuh"
+
+namespace afp {
+namespace {
+
+constexpr int BLK = 256;
+constexpr int WPB = BLK / 32;
+constexpr int MAXK = 64;
+constexpr int RED_GRID = 304;
+
+template <class X>
+struct AccT {
+  using type = float;
+};
+template <>
+struct AccT<double> {
+  using type = double;
+};
+template <class A, class V>
+__device__ __forceinline__ A as(V v) {
+  return (A)v;
+}
+template <>
+__device__ __forceinline__ float as<float, __nv_bfloat16>(__nv_bfloat16 v) {
+  return __bfloat162float(v);
+}
+
+__device__ __forceinline__ int64_t warp_id() { return ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ int64_t n_warps() { return ((int64_t)gridDim.x * blockDim.x) >> 5; }
+
+// y = A x or y += A x over n x k blocks
+template <int KPL, class V, class X, bool ADD>
+__global__ void k_spmm(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci, const V* __restrict__ va,
+                       const X* __restrict__ x, X* __restrict__ y, int k) {
+  using A = typename AccT<X>::type;
+  const int lane = threadIdx.x & 31;
+  for (int64_t row = warp_id(); row < m; row += n_warps()) {
+    A acc[KPL];
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) acc[q] = 0;
+    for (int j = rp[row]; j < rp[row + 1]; ++j) {
+      const A a = as<A>(va[j]);
+      const X* xr = x + (int64_t)ci[j] * k;
+#pragma unroll
+      for (int q = 0; q < KPL; ++q) {
+        const int c = lane + 32 * q;
+        if (c < k) acc[q] += a * (A)xr[c];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) {
+      const int c = lane + 32 * q;
+      if (c < k) {
+        X* o = y + row * k + c;
+        *o = ADD ? (X)((A)*o + acc[q]) : (X)acc[q];
+      }
+    }
+  }
+}
+
+template <int KPL, class X>
+__global__ void k_residual_m(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci,
+                             const X* __restrict__ va, const X* __restrict__ x, const X* __restrict__ r,
+                             X* __restrict__ out, int k) {
+  using A = typename AccT<X>::type;
+  const int lane = threadIdx.x & 31;
+  for (int64_t row = warp_id(); row < m; row += n_warps()) {
+    A acc[KPL];
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) acc[q] = 0;
+    for (int j = rp[row]; j < rp[row + 1]; ++j) {
+      const A a = (A)va[j];
+      const X* xr = x + (int64_t)ci[j] * k;
+#pragma unroll
+      for (int q = 0; q < KPL; ++q) {
+        const int c = lane + 32 * q;
+        if (c < k) acc[q] += a * (A)xr[c];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) {
+      const int c = lane + 32 * q;
+      if (c < k) out[row * k + c] = (X)((A)r[row * k + c] - acc[q]);
+    }
+  }
+}
+
+template <int KPL, class X>
+__global__ void k_gs_class_m(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
+                             const X* __restrict__ va, X* __restrict__ x, const X* __restrict__ r, int k) {
+  using A = typename AccT<X>::type;
+  const int lane = threadIdx.x & 31;
+  for (int64_t row = r0 + warp_id(); row < r1; row += n_warps()) {
+    A acc[KPL];
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) acc[q] = 0;
+    const int d = rp[row];
+    for (int j = d + 1; j < rp[row + 1]; ++j) {
+      const A a = (A)va[j];
+      const X* xr = x + (int64_t)ci[j] * k;
+#pragma unroll
+      for (int q = 0; q < KPL; ++q) {
+        const int c = lane + 32 * q;
+        if (c < k) acc[q] += a * (A)xr[c];
+      }
+    }
+    const A diag = (A)va[d];
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) {
+      const int c = lane + 32 * q;
+      if (c < k) x[row * k + c] = (X)(((A)r[row * k + c] - acc[q]) / diag);
+    }
+  }
+}
+
+template <int KPL, class X>
+__global__ void k_jacobi_l1_m(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
+                              const X* __restrict__ va, const X* __restrict__ x, const X* __restrict__ r,
+                              const X* __restrict__ d, X* __restrict__ tmp, int k) {
+  using A = typename AccT<X>::type;
+  const int lane = threadIdx.x & 31;
+  for (int64_t row = r0 + warp_id(); row < r1; row += n_warps()) {
+    A acc[KPL];
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) acc[q] = 0;
+    for (int j = rp[row]; j < rp[row + 1]; ++j) {
+      const A a = (A)va[j];
+      const X* xr = x + (int64_t)ci[j] * k;
+#pragma unroll
+      for (int q = 0; q < KPL; ++q) {
+        const int c = lane + 32 * q;
+        if (c < k) acc[q] += a * (A)xr[c];
+      }
+    }
+    const A dd = (A)d[row - r0];
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) {
+      const int c = lane + 32 * q;
+      if (c < k) tmp[(row - r0) * k + c] = (X)((A)x[row * k + c] + ((A)r[row * k + c] - acc[q]) / dd);
+    }
+  }
+}
+
+template <class X>
+__global__ void k_copy(int64_t n, const X* __restrict__ s, X* __restrict__ d) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] = s[i];
+}
+
+template <int KPL, class X>
+__global__ void k_dense_gemm(int64_t n, const X* __restrict__ M, const X* __restrict__ r, X* __restrict__ x, int k) {
+  using A = typename AccT<X>::type;
+  const int lane = threadIdx.x & 31;
+  for (int64_t row = warp_id(); row < n; row += n_warps()) {
+    A acc[KPL];
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) acc[q] = 0;
+    for (int64_t j = 0; j < n; ++j) {
+      const A a = (A)M[row * n + j];
+#pragma unroll
+      for (int q = 0; q < KPL; ++q) {
+        const int c = lane + 32 * q;
+        if (c < k) acc[q] += a * (A)r[j * k + c];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) {
+      const int c = lane + 32 * q;
+      if (c < k) x[row * k + c] = (X)acc[q];
+    }
+  }
+}
+
+template <class X>
+__global__ void k_diag_solve_m(int64_t n, const int* __restrict__ rp, const X* __restrict__ va,
+                               const X* __restrict__ r, X* __restrict__ x, int k) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n * k) x[t] = r[t] / va[rp[t / k]];
+}
+
+template <class A, class B>
+__global__ void k_conv(int64_t n, const A* __restrict__ in, B* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (B)in[i];
+}
+
+template <class X>
+__global__ void k_zero_m(int64_t n, X* __restrict__ x) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = (X)0;
+}
+
+// out row i = in row perm[i] (gather) or out row perm[i] = in row i (scatter)
+__global__ void k_rows_gather(int64_t n, int k, const int* __restrict__ perm, const double* __restrict__ in,
+                              int64_t ld_in, double* __restrict__ out) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  const int64_t i = t / k;
+  const int c = (int)(t % k);
+  out[t] = in[(int64_t)perm[i] * ld_in + c];
+}
+__global__ void k_rows_scatter(int64_t n, int k, const int* __restrict__ perm, const double* __restrict__ in,
+                               double* __restrict__ out, int64_t ld_out) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  const int64_t i = t / k;
+  const int c = (int)(t % k);
+  out[(int64_t)perm[i] * ld_out + c] = in[t];
+}
+
+// ------------------------------------------------------ column reductions
+// Per-column sums of a.b over n x k blocks; deterministic (block partials,
+// last block adds them in block order).
+// partials: the batch's [RED_GRID x MAXK] scratch, followed in memory by the
+// batch's retire counter (an unsigned in the next double slot)
+template <int KPL>
+__device__ void col_finish(double (&part)[KPL], int k, double* partials, double* dst) {
+  unsigned* retire = reinterpret_cast<unsigned*>(partials + (int64_t)RED_GRID * MAXK);
+  __shared__ double sm[WPB][MAXK];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < KPL; ++q) {
+    const int c = lane + 32 * q;
+    if (c < MAXK) sm[w][c] = part[q];
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < k; c += blockDim.x) {
+    double s = 0;
+    for (int ww = 0; ww < WPB; ++ww) s += sm[ww][c];
+    partials[(int64_t)blockIdx.x * MAXK + c] = s;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicInc(retire, gridDim.x - 1) == gridDim.x - 1);
+  __syncthreads();
+  if (last) {
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+      double s = 0;
+      for (unsigned b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[(int64_t)b * MAXK + c];
+      dst[c] = s;
+    }
+  }
+}
+
+template <int KPL>
+__global__ void k_col_dot(int64_t n, const double* __restrict__ a, const double* __restrict__ b, int k,
+                          double* partials, double* dst) {
+  const int lane = threadIdx.x & 31;
+  double part[KPL];
+#pragma unroll
+  for (int q = 0; q < KPL; ++q) part[q] = 0;
+  for (int64_t row = warp_id(); row < n; row += n_warps()) {
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) {
+      const int c = lane + 32 * q;
+      if (c < k) part[q] += a[row * k + c] * b[row * k + c];
+    }
+  }
+  col_finish<KPL>(part, k, partials, dst);
+}
+
+template <int KPL>
+__global__ void k_spmm_dot(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci,
+                           const double* __restrict__ va, const double* __restrict__ p, double* __restrict__ q_out,
+                           int k, double* partials, double* dst) {
+  const int lane = threadIdx.x & 31;
+  double part[KPL];
+#pragma unroll
+  for (int q = 0; q < KPL; ++q) part[q] = 0;
+  for (int64_t row = warp_id(); row < m; row += n_warps()) {
+    double acc[KPL];
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) acc[q] = 0;
+    for (int j = rp[row]; j < rp[row + 1]; ++j) {
+      const double a = va[j];
+      const double* pr = p + (int64_t)ci[j] * k;
+#pragma unroll
+      for (int q = 0; q < KPL; ++q) {
+        const int c = lane + 32 * q;
+        if (c < k) acc[q] += a * pr[c];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) {
+      const int c = lane + 32 * q;
+      if (c < k) {
+        q_out[row * k + c] = acc[q];
+        part[q] += acc[q] * p[row * k + c];
+      }
+    }
+  }
+  col_finish<KPL>(part, k, partials, dst);
+}
+
+// x += alpha_c p, r -= alpha_c q for active columns; rr_c = r.r
+template <int KPL>
+__global__ void k_update_xr(int64_t n, int k, const double* __restrict__ num, const double* __restrict__ den,
+                            const int* __restrict__ active, double* __restrict__ x, double* __restrict__ r,
+                            const double* __restrict__ p, const double* __restrict__ q, double* partials,
+                            double* dst) {
+  const int lane = threadIdx.x & 31;
+  double alpha[KPL], part[KPL];
+#pragma unroll
+  for (int t = 0; t < KPL; ++t) {
+    const int c = lane + 32 * t;
+    alpha[t] = (c < k && active[c]) ? num[c] / den[c] : 0.0;
+    part[t] = 0;
+  }
+  for (int64_t row = warp_id(); row < n; row += n_warps()) {
+#pragma unroll
+    for (int t = 0; t < KPL; ++t) {
+      const int c = lane + 32 * t;
+      if (c < k) {
+        const int64_t o = row * k + c;
+        x[o] += alpha[t] * p[o];
+        const double rv = r[o] - alpha[t] * q[o];
+        r[o] = rv;
+        part[t] += rv * rv;
+      }
+    }
+  }
+  col_finish<KPL>(part, k, partials, dst);
+}
+
+template <int KPL>
+__global__ void k_update_p(int64_t n, int k, const double* __restrict__ num, const double* __restrict__ den,
+                           const int* __restrict__ active, const double* __restrict__ z, double* __restrict__ p) {
+  const int lane = threadIdx.x & 31;
+  double beta[KPL];
+  bool act[KPL];
+#pragma unroll
+  for (int t = 0; t < KPL; ++t) {
+    const int c = lane + 32 * t;
+    act[t] = c < k && active[c];
+    beta[t] = act[t] ? num[c] / den[c] : 0.0;
+  }
+  for (int64_t row = warp_id(); row < n; row += n_warps()) {
+#pragma unroll
+    for (int t = 0; t < KPL; ++t) {
+      const int c = lane + 32 * t;
+      if (c < k && act[t]) p[row * k + c] = z[row * k + c] + beta[t] * p[row * k + c];
+    }
+  }
+}
+
+unsigned rows_grid(const afp_context* ctx, int64_t rows) {
+  const int64_t want = (rows + WPB - 1) / WPB;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->sm_count * 16));
+}
+
+template <class F>
+void with_kpl(int k, F&& f) {
+  if (k <= 32) f(std::integral_constant<int, 1>());
+  else f(std::integral_constant<int, 2>());
+}
+
+// ---------------------------------------------------------------- V-cycle
+template <class X>
+X* blk(MultiState& S, int which, int l);
+template <>
+double* blk<double>(MultiState& S, int which, int l) {
+  return (which == 0 ? S.X : which == 1 ? S.R : S.T)[l].get();
+}
+template <>
+float* blk<float>(MultiState& S, int which, int l) {
+  return (which == 0 ? S.X32 : which == 1 ? S.R32 : S.T32)[l].get();
+}
+
+template <class X, class PV>
+void vcycle_m(afp_amg* h, MultiState& S) {
+  const afp_context* ctx = h->ctx;
+  const int k = S.k, t = h->t;
+  with_kpl(k, [&](auto KPLc) {
+    constexpr int KPL = decltype(KPLc)::value;
+    auto smooth = [&](int l, X* x, const X* r, bool backward) {
+      const Level& L = h->lv[l];
+      CSRView<X> A = L.A<X>();
+      const int K = (int)L.cls.size() - 1;
+      for (int s = 0; s < h->opts.smooth_step; ++s)
+        for (int q = 0; q < K; ++q) {
+          const int c = backward ? K - 1 - q : q;
+          const int64_t r0 = L.cls[c], r1 = L.cls[c + 1];
+          if (r1 <= r0) continue;
+          if (L.overflow && c == K - 1) {
+            const X* d;
+            if constexpr (std::is_same<X, double>::value) d = L.l1d.get();
+            else d = L.l1d32.get();
+            X* tmp = blk<X>(S, 2, l);
+            k_jacobi_l1_m<KPL, X><<<rows_grid(ctx, r1 - r0), BLK, 0, ctx->stream>>>(r0, r1, A.rowptr, A.cols, A.vals,
+                                                                                   x, r, d, tmp, k);
+            check_launch(ctx, "mrhs l1-jacobi");
+            k_copy<X><<<grid_for((r1 - r0) * k, BLK), BLK, 0, ctx->stream>>>((r1 - r0) * k, tmp, x + r0 * k);
+            check_launch(ctx, "mrhs copy");
+          } else {
+            k_gs_class_m<KPL, X><<<rows_grid(ctx, r1 - r0), BLK, 0, ctx->stream>>>(r0, r1, A.rowptr, A.cols, A.vals,
+                                                                                  x, r, k);
+            check_launch(ctx, "mrhs gauss-seidel class");
+          }
+        }
+    };
+    for (int l = 0; l < t; ++l) {
+      Level& L = h->lv[l];
+      X* x = blk<X>(S, 0, l);
+      const X* r = blk<X>(S, 1, l);
+      k_zero_m<X><<<grid_for(L.n * k, BLK), BLK, 0, ctx->stream>>>(L.n * k, x);
+      check_launch(ctx, "mrhs zero");
+      smooth(l, x, r, false);
+      CSRView<X> A = L.A<X>();
+      k_residual_m<KPL, X><<<rows_grid(ctx, L.n), BLK, 0, ctx->stream>>>(L.n, A.rowptr, A.cols, A.vals, x, r,
+                                                                        blk<X>(S, 2, l), k);
+      check_launch(ctx, "mrhs residual");
+      const PV* pv;
+      if constexpr (std::is_same<PV, double>::value) pv = L.pva.get();
+      else pv = L.pva16.get();
+      const int64_t nc = h->lv[l + 1].n;
+      k_spmm<KPL, PV, X, false><<<rows_grid(ctx, nc), BLK, 0, ctx->stream>>>(nc, L.prp.get(), L.pci.get(), pv,
+                                                                            blk<X>(S, 2, l), blk<X>(S, 1, l + 1), k);
+      check_launch(ctx, "mrhs restriction");
+    }
+    const Level& T = h->lv[t];
+    if (h->tail_dense) {
+      const X* inv;
+      if constexpr (std::is_same<X, double>::value) inv = h->tail_inv.get();
+      else inv = h->tail_inv32.get();
+      k_dense_gemm<KPL, X><<<rows_grid(ctx, T.n), BLK, 0, ctx->stream>>>(T.n, inv, blk<X>(S, 1, t), blk<X>(S, 0, t), k);
+      check_launch(ctx, "mrhs dense tail");
+    } else {
+      CSRView<X> A = T.A<X>();
+      k_diag_solve_m<X><<<grid_for(T.n * k, BLK), BLK, 0, ctx->stream>>>(T.n, A.rowptr, A.vals, blk<X>(S, 1, t),
+                                                                         blk<X>(S, 0, t), k);
+      check_launch(ctx, "mrhs diagonal tail");
+    }
+    for (int l = t - 1; l >= 0; --l) {
+      Level& L = h->lv[l];
+      const PV* tv;
+      if constexpr (std::is_same<PV, double>::value) tv = L.tva.get();
+      else tv = L.tva16.get();
+      k_spmm<KPL, PV, X, true><<<rows_grid(ctx, L.n), BLK, 0, ctx->stream>>>(L.n, L.trp.get(), L.tci.get(), tv,
+                                                                            blk<X>(S, 0, l + 1), blk<X>(S, 0, l), k);
+      check_launch(ctx, "mrhs prolongation");
+      smooth(l, blk<X>(S, 0, l), blk<X>(S, 1, l), h->opts.symmetric != 0);
+    }
+  });
+}
+
+void ensure_state(afp_amg* h, int k) {
+  const bool mixed = h->opts.precision == AFP_PRECISION_MIXED;
+  if (h->multi && h->multi->k == k && h->multi->mixed == mixed) return;
+  afp_context* ctx = h->ctx;
+  auto S = std::make_unique<MultiState>();
+  S->k = k;
+  S->mixed = mixed;
+  const int L = h->t + 1;
+  if (mixed) {
+    S->X32.resize(L);
+    S->R32.resize(L);
+    S->T32.resize(L);
+  } else {
+    S->X.resize(L);
+    S->R.resize(L);
+    S->T.resize(L);
+  }
+  for (int l = 0; l < L; ++l) {
+    const int64_t nk = h->lv[l].n * k;
+    if (mixed) {
+      S->X32[l].alloc(ctx, nk);
+      S->R32[l].alloc(ctx, nk);
+      S->T32[l].alloc(ctx, nk);
+    } else {
+      S->X[l].alloc(ctx, nk);
+      S->R[l].alloc(ctx, nk);
+      S->T[l].alloc(ctx, nk);
+    }
+  }
+  const int64_t n0k = h->lv[0].n * k;
+  S->B.alloc(ctx, n0k);
+  S->Xs.alloc(ctx, n0k);
+  S->Rs.alloc(ctx, n0k);
+  S->Z.alloc(ctx, n0k);
+  S->P.alloc(ctx, n0k);
+  S->Q.alloc(ctx, n0k);
+  S->Tmp.alloc(ctx, n0k);
+  S->scal.alloc(ctx, 8 * MAXK + (int64_t)RED_GRID * MAXK + 1);  // scalars, partials, retire counter
+  S->scal.zero();
+  S->active.alloc(ctx, MAXK);
+  h->multi = std::move(S);
+}
+
+// Z = V(R) for all columns, through a captured graph.
+void precondition_m(afp_amg* h) {
+  afp_context* ctx = h->ctx;
+  MultiState& S = *h->multi;
+  const int64_t n0k = h->lv[0].n * S.k;
+  if (S.graph == nullptr) {
+    cudaGraph_t g;
+    const int64_t before = ctx->launches.n;
+    AFP_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      if (S.mixed) {
+        k_conv<double, float><<<grid_for(n0k, BLK), BLK, 0, ctx->stream>>>(n0k, S.Rs.get(), S.R32[0].get());
+        check_launch(ctx, "mrhs to fp32");
+        vcycle_m<float, __nv_bfloat16>(h, S);
+        k_conv<float, double><<<grid_for(n0k, BLK), BLK, 0, ctx->stream>>>(n0k, S.X32[0].get(), S.Z.get());
+        check_launch(ctx, "mrhs to fp64");
+      } else {
+        k_copy<double><<<grid_for(n0k, BLK), BLK, 0, ctx->stream>>>(n0k, S.Rs.get(), S.R[0].get());
+        check_launch(ctx, "mrhs copy r");
+        vcycle_m<double, double>(h, S);
+        k_copy<double><<<grid_for(n0k, BLK), BLK, 0, ctx->stream>>>(n0k, S.X[0].get(), S.Z.get());
+        check_launch(ctx, "mrhs copy z");
+      }
+    } catch (...) {
+      cudaStreamEndCapture(ctx->stream, &g);
+      throw;
+    }
+    AFP_CUDA(cudaStreamEndCapture(ctx->stream, &g));
+    AFP_CUDA(cudaGraphInstantiate(&S.graph, g, 0));
+    AFP_CUDA(cudaGraphDestroy(g));
+    S.graph_nodes = ctx->launches.n - before;
+    ctx->launches.n = before;
+  }
+  AFP_CUDA(cudaGraphLaunch(S.graph, ctx->stream));
+  ctx->launches.n += S.graph_nodes;
+}
+
+}  // namespace
+
+// Batched CG over up to 64 columns (callers chunk wider blocks).
+void pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, double tol, int maxit,
+               afp_solve_info* info) {
+  afp_context* ctx = h->ctx;
+  const int k = nrhs;
+  AFP_REQUIRE(k >= 1 && k <= MAXK, AFP_ERR_INVALID, "at most 64 columns per batch");
+  ensure_state(h, k);
+  MultiState& S = *h->multi;
+  const Level& L0 = h->lv[0];
+  const int64_t n = L0.n, nk = n * k;
+  double* sc = S.scal.get();  // rows: 0 rz_a, 1 pq, 2 rr, 3 rz_b, 4 bb
+  double* partials = sc + 8 * MAXK;
+  cudaEvent_t e0, e1;
+  AFP_CUDA(cudaEventCreate(&e0));
+  AFP_CUDA(cudaEventCreate(&e1));
+  // inputs into solve order (caller's arrays may be host or device)
+  copy(ctx, S.Tmp.get(), B_user, sizeof(double) * nk);
+  AFP_CUDA(cudaEventRecord(e0, ctx->stream));
+  k_rows_gather<<<grid_for(nk, BLK), BLK, 0, ctx->stream>>>(n, k, L0.perm.get(), S.Tmp.get(), k, S.B.get());
+  check_launch(ctx, "mrhs gather b");
+  copy(ctx, S.Tmp.get(), X_user, sizeof(double) * nk);
+  k_rows_gather<<<grid_for(nk, BLK), BLK, 0, ctx->stream>>>(n, k, L0.perm.get(), S.Tmp.get(), k, S.Xs.get());
+  check_launch(ctx, "mrhs gather x");
+  std::vector<int> act(k, 1);
+  S.active.upload(act.data(), k);
+  const CSRView<double> A = L0.A<double>();
+  const unsigned rg = std::min<unsigned>(RED_GRID, rows_grid(ctx, n));
+  with_kpl(k, [&](auto KPLc) {
+    constexpr int KPL = decltype(KPLc)::value;
+    k_residual_m<KPL, double><<<rows_grid(ctx, n), BLK, 0, ctx->stream>>>(n, A.rowptr, A.cols, A.vals, S.Xs.get(),
+                                                                          S.B.get(), S.Rs.get(), k);
+    check_launch(ctx, "mrhs residual");
+    k_col_dot<KPL><<<rg, BLK, 0, ctx->stream>>>(n, S.B.get(), S.B.get(), k, partials, sc + 4 * MAXK);
+    check_launch(ctx, "mrhs dot");
+    k_col_dot<KPL><<<rg, BLK, 0, ctx->stream>>>(n, S.Rs.get(), S.Rs.get(), k, partials, sc + 2 * MAXK);
+    check_launch(ctx, "mrhs dot");
+  });
+  std::vector<double> hb(k), hr(k), init(k), rel(k);
+  copy(ctx, hb.data(), sc + 4 * MAXK, sizeof(double) * k);
+  copy(ctx, hr.data(), sc + 2 * MAXK, sizeof(double) * k);
+  sync(ctx);
+  std::vector<double> bn(k);
+  int n_active = 0;
+  std::vector<int> iters(k, 0);
+  for (int c = 0; c < k; ++c) {
+    bn[c] = std::max(std::sqrt(hb[c]), 1e-30);
+    rel[c] = init[c] = std::sqrt(hr[c]) / bn[c];
+    if (!std::isfinite(rel[c])) fail(AFP_ERR_BREAKDOWN, "non-finite initial residual");
+    act[c] = rel[c] > tol;
+    n_active += act[c];
+  }
+  S.active.upload(act.data(), k);
+  int it = 0;
+  if (n_active > 0) {
+    precondition_m(h);
+    int cur = 0, nxt = 3;
+    with_kpl(k, [&](auto KPLc) {
+      constexpr int KPL = decltype(KPLc)::value;
+      k_col_dot<KPL><<<rg, BLK, 0, ctx->stream>>>(n, S.Rs.get(), S.Z.get(), k, partials, sc + cur * MAXK);
+      check_launch(ctx, "mrhs dot");
+    });
+    AFP_CUDA(cudaMemcpyAsync(S.P.get(), S.Z.get(), sizeof(double) * nk, cudaMemcpyDeviceToDevice, ctx->stream));
+    for (it = 1; it <= maxit; ++it) {
+      with_kpl(k, [&](auto KPLc) {
+        constexpr int KPL = decltype(KPLc)::value;
+        k_spmm_dot<KPL><<<rg, BLK, 0, ctx->stream>>>(n, A.rowptr, A.cols, A.vals, S.P.get(), S.Q.get(), k, partials,
+                                                     sc + 1 * MAXK);
+        check_launch(ctx, "mrhs spmm+dot");
+        k_update_xr<KPL><<<rg, BLK, 0, ctx->stream>>>(n, k, sc + cur * MAXK, sc + 1 * MAXK, S.active.get(),
+                                                      S.Xs.get(), S.Rs.get(), S.P.get(), S.Q.get(), partials,
+                                                      sc + 2 * MAXK);
+        check_launch(ctx, "mrhs update x r");
+      });
+      copy(ctx, hr.data(), sc + 2 * MAXK, sizeof(double) * k);
+      sync(ctx);
+      n_active = 0;
+      for (int c = 0; c < k; ++c) {
+        if (!act[c]) continue;
+        rel[c] = std::sqrt(hr[c]) / bn[c];
+        if (!std::isfinite(rel[c])) fail(AFP_ERR_BREAKDOWN, "non-finite residual");
+        iters[c] = it;
+        if (rel[c] <= tol) act[c] = 0;
+        n_active += act[c];
+      }
+      if (n_active == 0) break;
+      S.active.upload(act.data(), k);
+      precondition_m(h);
+      with_kpl(k, [&](auto KPLc) {
+        constexpr int KPL = decltype(KPLc)::value;
+        k_col_dot<KPL><<<rg, BLK, 0, ctx->stream>>>(n, S.Rs.get(), S.Z.get(), k, partials, sc + nxt * MAXK);
+        check_launch(ctx, "mrhs dot");
+        k_update_p<KPL><<<rows_grid(ctx, n), BLK, 0, ctx->stream>>>(n, k, sc + nxt * MAXK, sc + cur * MAXK,
+                                                                     S.active.get(), S.Z.get(), S.P.get());
+        check_launch(ctx, "mrhs update p");
+      });
+      std::swap(cur, nxt);
+    }
+    if (it > maxit) it = maxit;
+  }
+  k_rows_scatter<<<grid_for(nk, BLK), BLK, 0, ctx->stream>>>(n, k, L0.perm.get(), S.Xs.get(), S.Tmp.get(), k);
+  check_launch(ctx, "mrhs scatter x");
+  AFP_CUDA(cudaEventRecord(e1, ctx->stream));
+  copy(ctx, X_user, S.Tmp.get(), sizeof(double) * nk);
+  sync(ctx);
+  float ms = 0;
+  AFP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (info)
+    for (int c = 0; c < k; ++c) {
+      info[c].iterations = iters[c];
+      info[c].converged = rel[c] <= tol;
+      info[c].initial_residual = init[c];
+      info[c].final_residual = rel[c];
+      info[c].seconds = ms * 1e-3;
+    }
+}
+
+}  // namespace afp

@@ -183,8 +183,11 @@ __global__ void k_zero(int64_t n, X* __restrict__ x) {
 // ------------------------------------------------------------ reductions
 constexpr int RED_BLOCKS = 512;
 
-__device__ unsigned int g_retire = 0;
-__device__ double g_partials[RED_BLOCKS];
+// the context's partials array (RED_BLOCKS entries) and retire counter
+struct RedScratch {
+  double* partials;
+  unsigned* retire;
+};
 
 __device__ __forceinline__ double block_sum(double v) {
   __shared__ double ws[BLK / 32];
@@ -201,35 +204,36 @@ __device__ __forceinline__ double block_sum(double v) {
   return s;  // valid in thread 0
 }
 
-// Partial of this block -> g_partials; the last block sums them in order.
-__device__ __forceinline__ void finish_reduction(double partial, double* dst) {
+// Partial of this block -> scratch; the last block sums them in order.
+__device__ __forceinline__ void finish_reduction(double partial, double* dst, RedScratch rs) {
   __shared__ bool last;
   if (threadIdx.x == 0) {
-    g_partials[blockIdx.x] = partial;
+    rs.partials[blockIdx.x] = partial;
     __threadfence();
-    unsigned done = atomicInc(&g_retire, gridDim.x - 1);  // wraps to 0 for the last block
+    unsigned done = atomicInc(rs.retire, gridDim.x - 1);  // wraps to 0 for the last block
     last = (done == gridDim.x - 1);
   }
   __syncthreads();
   if (last) {
     double s = 0;
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += BLK) s += ((volatile double*)g_partials)[b];
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += BLK) s += ((volatile double*)rs.partials)[b];
     s = block_sum(s);
     if (threadIdx.x == 0) *dst = s;
   }
 }
 
-__global__ void k_dot(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* dst) {
+__global__ void k_dot(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* dst,
+                      RedScratch rs) {
   double s = 0;
   for (int64_t i = (int64_t)blockIdx.x * BLK + threadIdx.x; i < n; i += (int64_t)gridDim.x * BLK) s += a[i] * b[i];
   s = block_sum(s);
-  finish_reduction(s, dst);
+  finish_reduction(s, dst, rs);
 }
 
 template <int VEC>
 __global__ void k_spmv_dot(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci,
                            const double* __restrict__ va, const double* __restrict__ p, double* __restrict__ y,
-                           double* dst) {
+                           double* dst, RedScratch rs) {
   // warps stride over the rows uniformly so every lane joins each shuffle
   constexpr int GPW = 32 / VEC;
   const int lane = threadIdx.x % VEC, sub = (threadIdx.x & 31) / VEC;
@@ -247,12 +251,12 @@ __global__ void k_spmv_dot(int64_t m, const int* __restrict__ rp, const int* __r
     }
   }
   part = block_sum(part);
-  finish_reduction(part, dst);
+  finish_reduction(part, dst, rs);
 }
 
 __global__ void k_cg_update_xr(int64_t n, const double* __restrict__ sc, int num, int den, double* __restrict__ x,
                                double* __restrict__ r, const double* __restrict__ p, const double* __restrict__ q,
-                               double* dst) {
+                               double* dst, RedScratch rs) {
   const double alpha = sc[num] / sc[den];
   double s = 0;
   for (int64_t i = (int64_t)blockIdx.x * BLK + threadIdx.x; i < n; i += (int64_t)gridDim.x * BLK) {
@@ -262,7 +266,7 @@ __global__ void k_cg_update_xr(int64_t n, const double* __restrict__ sc, int num
     s += ri * ri;
   }
   s = block_sum(s);
-  finish_reduction(s, dst);
+  finish_reduction(s, dst, rs);
 }
 
 __global__ void k_cg_update_p(int64_t n, const double* __restrict__ sc, int num, int den, const double* __restrict__ z,
@@ -481,21 +485,23 @@ void fill_zero(const afp_context* ctx, int64_t n, X* x) {
 }
 
 void dot(const afp_context* ctx, int64_t n, const double* a, const double* b, double* dst) {
-  k_dot<<<red_grid(ctx, n), BLK, 0, ctx->stream>>>(n, a, b, dst);
+  k_dot<<<red_grid(ctx, n), BLK, 0, ctx->stream>>>(n, a, b, dst, RedScratch{ctx->d_partials, ctx->d_retire});
   check_launch(ctx, "dot");
 }
 
 void spmv_dot(const afp_context* ctx, const CSRView<double>& A, const double* p, double* y, double* dst) {
   launch_vec(A.vec, [&](auto VEC) {
     constexpr int W = decltype(VEC)::value;
-    k_spmv_dot<W><<<red_grid(ctx, A.m * W), BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.cols, A.vals, p, y, dst);
+    k_spmv_dot<W><<<red_grid(ctx, A.m * W), BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.cols, A.vals, p, y, dst,
+                                                                   RedScratch{ctx->d_partials, ctx->d_retire});
   });
   check_launch(ctx, "spmv+dot");
 }
 
 void cg_update_xr(const afp_context* ctx, int64_t n, const double* s, int num, int den, double* x, double* r,
                   const double* p, const double* q, double* dst) {
-  k_cg_update_xr<<<red_grid(ctx, n), BLK, 0, ctx->stream>>>(n, s, num, den, x, r, p, q, dst);
+  k_cg_update_xr<<<red_grid(ctx, n), BLK, 0, ctx->stream>>>(n, s, num, den, x, r, p, q, dst,
+                                                            RedScratch{ctx->d_partials, ctx->d_retire});
   check_launch(ctx, "cg update x r");
 }
 

@@ -93,6 +93,12 @@ class SparseMatrix:
         N.call("afp_matrix_download", self.handle, N.ptr(rp), N.ptr(ci), N.ptr(va))
         return rp, ci, va
 
+    def set_values(self, vals):
+        """Overwrite the stored values (pattern unchanged)."""
+        if not hasattr(vals, "data_ptr"):
+            vals = np.ascontiguousarray(vals, dtype=np.float64)
+        N.call("afp_matrix_set_values", self.handle, N.ptr(vals))
+
     def values(self):
         _, _, nnz = self.info()
         va = np.empty(nnz, dtype=np.float64)

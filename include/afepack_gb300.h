@@ -101,6 +101,9 @@ afp_status afp_matrix_create_csr(afp_context *ctx, int64_t m, int64_t n, int64_t
                                  const int32_t *rowptr, const int32_t *cols, const double *vals,
                                  afp_matrix **out);
 afp_status afp_matrix_info(const afp_matrix *a, int64_t *m, int64_t *n, int64_t *nnz);
+/* Overwrites all nnz stored values, keeping the pattern (what writing
+ * SparseMatrix::global_entry(k) does in the reference). */
+afp_status afp_matrix_set_values(afp_matrix *a, const double *vals);
 /* Copies the pattern and values out (any argument may be NULL to skip). */
 afp_status afp_matrix_download(const afp_matrix *a, int32_t *rowptr, int32_t *cols, double *vals);
 /* y = A x  (SparseMatrix::vmult, include/AFEPack/SparseMatrix.h:100-114) */
@@ -152,6 +155,17 @@ void afp_amg_default_opts(afp_amg_opts *opts);
  * getPMPt (:288-358) on the GPU, level by level, until the reference's stop
  * rule (order <= max_coarse and density >= min_density) holds. */
 afp_status afp_amg_setup(afp_matrix *a, const afp_amg_opts *opts, afp_amg **out);
+/* AMGSolver::lazyReinit on a fresh solver, i.e. lazyInit (src/AMGSolver.cpp:442-503):
+ * the hierarchy of lazyProject (:235-284, aggregation-like P with 1/count
+ * weights), which AMGPreconditioner uses. */
+afp_status afp_amg_setup_lazy(afp_matrix *a, const afp_amg_opts *opts, afp_amg **out);
+/* AMGSolver::lazyReinit on an initialised lazy solver (:505-545): the same
+ * projections applied to new matrix values.  `a` must share the pattern
+ * object the solver was set up with -- the same matrix after
+ * afp_matrix_set_values, or the stiffness/mass pair of one afp_assemble
+ * call -- otherwise AFP_ERR_INVALID, as the reference aborts.  Only the GPU
+ * Galerkin products run; no host C/F splitting. */
+afp_status afp_amg_lazy_reinit(afp_amg *amg, afp_matrix *a);
 afp_status afp_amg_destroy(afp_amg *amg);
 afp_status afp_amg_num_levels(const afp_amg *amg, int *n_project, int *solve_levels);
 /* level l (0 = fine): order, stored entries, smoother colour classes

@@ -235,9 +235,18 @@ static void matrix_add(orc_csr *a, int64_t i, int64_t j, double v) {
 
 /* SparseMatrix::el -- 0 when (i,j) is not in the pattern */
 static double matrix_el(const orc_csr *a, int64_t i, int64_t j) {
-  for (int64_t k = a->rowptr[i]; k < a->rowptr[i + 1]; ++k)
-    if (a->cols[k] == j) return a->vals[k];
-  return 0;
+  /* rows are [diagonal, ascending others] (square) or ascending (rectangular):
+   * a binary search over the sorted part finds the entry the reference's
+   * linear scan finds */
+  int64_t b = a->rowptr[i], e = a->rowptr[i + 1];
+  if (b == e) return 0;
+  if (a->cols[b] == j) return a->vals[b];
+  int64_t lo = b + 1, hi = e;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) / 2;
+    if (a->cols[mid] < j) lo = mid + 1; else hi = mid;
+  }
+  return (lo < e && a->cols[lo] == j) ? a->vals[lo] : 0;
 }
 
 int orc_assemble(int dim, int degree, const double *coords, int64_t n_cell, const int64_t *cells,
@@ -333,65 +342,78 @@ void orc_apply_dirichlet(orc_csr *a, double *f, const int32_t *dirichlet, const 
 /* AMG (src/AMGSolver.cpp)                                                  */
 /* ------------------------------------------------------------------------ */
 
-/* getPMPt (src/AMGSolver.cpp:288-358) */
+/* getPMPt (src/AMGSolver.cpp:288-358).  Rows are independent: each row's
+ * column set is the reference's (diagonal first, then ascending after
+ * SparsityPattern::compress) and each entry is accumulated serially in the
+ * reference's (j, k, l) order, so running rows on several threads (OpenMP)
+ * changes nothing in the result. */
 static int rap_with_pt(const orc_csr *P, const orc_csr *M, const orc_csr *Pt, orc_csr *A) {
   const int64_t nc = P->m;
-  int64_t *row_length = (int64_t *)calloc(nc, sizeof(int64_t));
-  char *flag = (char *)malloc(nc ? nc : 1);
-  int64_t *index = (int64_t *)malloc(sizeof(int64_t) * (nc ? nc : 1));
-  int64_t **col_index = (int64_t **)calloc(nc ? nc : 1, sizeof(int64_t *));
-  memset(flag, 1, nc);
-  for (int64_t i = 0; i < nc; ++i) {
-    row_length[i] = 1;
-    flag[i] = 0;
-    index[0] = i;
-    for (int64_t j = P->rowptr[i]; j < P->rowptr[i + 1]; ++j) {
-      int64_t a = P->cols[j];
-      for (int64_t k = M->rowptr[a]; k < M->rowptr[a + 1]; ++k) {
-        int64_t b = M->cols[k];
-        for (int64_t l = Pt->rowptr[b]; l < Pt->rowptr[b + 1]; ++l) {
-          int64_t c = Pt->cols[l];
-          if (flag[c]) { index[row_length[i]++] = c; flag[c] = 0; }
+  A->m = A->n = nc;
+  A->rowptr = (int64_t *)calloc(nc + 1, sizeof(int64_t));
+  /* pass 1: row lengths */
+#pragma omp parallel
+  {
+    char *flag = (char *)calloc(nc ? nc : 1, 1);
+    int64_t *index = (int64_t *)malloc(sizeof(int64_t) * (nc ? nc : 1));
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t i = 0; i < nc; ++i) {
+      int64_t len = 1;
+      flag[i] = 1;
+      index[0] = i;
+      for (int64_t j = P->rowptr[i]; j < P->rowptr[i + 1]; ++j) {
+        int64_t a = P->cols[j];
+        for (int64_t k = M->rowptr[a]; k < M->rowptr[a + 1]; ++k) {
+          int64_t b = M->cols[k];
+          for (int64_t l = Pt->rowptr[b]; l < Pt->rowptr[b + 1]; ++l) {
+            int64_t c = Pt->cols[l];
+            if (!flag[c]) { index[len++] = c; flag[c] = 1; }
+          }
         }
       }
+      for (int64_t q = 0; q < len; ++q) flag[index[q]] = 0;
+      A->rowptr[i + 1] = len;
     }
-    col_index[i] = (int64_t *)malloc(sizeof(int64_t) * row_length[i]);
-    for (int64_t j = 0; j < row_length[i]; ++j) { col_index[i][j] = index[j]; flag[index[j]] = 1; }
+    free(flag);
+    free(index);
   }
-  /* SparsityPattern(nc, row_length) + add + compress */
-  int64_t *slot_start = (int64_t *)malloc(sizeof(int64_t) * (nc + 1));
-  slot_start[0] = 0;
-  for (int64_t i = 0; i < nc; ++i) slot_start[i + 1] = slot_start[i] + row_length[i];
-  int64_t *slots = (int64_t *)malloc(sizeof(int64_t) * (slot_start[nc] ? slot_start[nc] : 1));
-  for (int64_t k = 0; k < slot_start[nc]; ++k) slots[k] = INVALID;
-  for (int64_t i = 0; i < nc; ++i) slots[slot_start[i]] = i;
-  for (int64_t i = 0; i < nc; ++i)
-    for (int64_t j = 0; j < row_length[i]; ++j) pattern_add(slots, slot_start[i], slot_start[i + 1], col_index[i][j]);
-  A->m = A->n = nc;
-  pattern_compress(nc, 1, slot_start, slots, A);
-  free(slots);
-  free(slot_start);
-  double *row_entry = (double *)calloc(nc ? nc : 1, sizeof(double));
-  for (int64_t i = 0; i < nc; ++i) {
-    for (int64_t j = P->rowptr[i]; j < P->rowptr[i + 1]; ++j) {
-      int64_t a = P->cols[j];
-      for (int64_t k = M->rowptr[a]; k < M->rowptr[a + 1]; ++k) {
-        int64_t b = M->cols[k];
-        for (int64_t l = Pt->rowptr[b]; l < Pt->rowptr[b + 1]; ++l)
-          row_entry[Pt->cols[l]] += P->vals[j] * M->vals[k] * Pt->vals[l];
+  for (int64_t i = 0; i < nc; ++i) A->rowptr[i + 1] += A->rowptr[i];
+  const int64_t nnz = A->rowptr[nc];
+  A->cols = (int64_t *)malloc(sizeof(int64_t) * (nnz ? nnz : 1));
+  A->vals = (double *)calloc(nnz ? nnz : 1, sizeof(double));
+  /* pass 2: pattern [i, ascending others] and values */
+#pragma omp parallel
+  {
+    char *flag = (char *)calloc(nc ? nc : 1, 1);
+    double *row_entry = (double *)calloc(nc ? nc : 1, sizeof(double));
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t i = 0; i < nc; ++i) {
+      int64_t *out = A->cols + A->rowptr[i];
+      int64_t len = 1;
+      out[0] = i;
+      flag[i] = 1;
+      for (int64_t j = P->rowptr[i]; j < P->rowptr[i + 1]; ++j) {
+        int64_t a = P->cols[j];
+        for (int64_t k = M->rowptr[a]; k < M->rowptr[a + 1]; ++k) {
+          int64_t b = M->cols[k];
+          for (int64_t l = Pt->rowptr[b]; l < Pt->rowptr[b + 1]; ++l) {
+            int64_t c = Pt->cols[l];
+            row_entry[c] += P->vals[j] * M->vals[k] * Pt->vals[l];
+            if (!flag[c]) { out[len++] = c; flag[c] = 1; }
+          }
+        }
+      }
+      if (len > 2) qsort(out + 1, len - 1, sizeof(int64_t), cmp_i64);
+      double *vo = A->vals + A->rowptr[i];
+      for (int64_t q = 0; q < len; ++q) {
+        vo[q] = 0.0 + row_entry[out[q]];
+        row_entry[out[q]] = 0.0;
+        flag[out[q]] = 0;
       }
     }
-    for (int64_t j = 0; j < row_length[i]; ++j) {
-      matrix_add(A, i, col_index[i][j], row_entry[col_index[i][j]]);
-      row_entry[col_index[i][j]] = 0.0;
-    }
-    free(col_index[i]);
+    free(flag);
+    free(row_entry);
   }
-  free(row_entry);
-  free(col_index);
-  free(index);
-  free(flag);
-  free(row_length);
   return 0;
 }
 
@@ -658,9 +680,152 @@ int orc_amg_setup(const orc_csr *a, int smooth_step, int64_t max_coarse, double 
   return 0;
 }
 
+int orc_amg_from_levels(int n_level, const orc_csr *A, const orc_csr *P, int most_project_full,
+                        int smooth_step, orc_amg *h) {
+  memset(h, 0, sizeof(*h));
+  h->smooth_step = smooth_step;
+  h->alpha = 0.25;
+  h->n_level = n_level;
+  h->most_project_full = most_project_full;
+  h->A = (orc_csr *)calloc(n_level + 1, sizeof(orc_csr));
+  h->P = (orc_csr *)calloc(n_level > 0 ? n_level : 1, sizeof(orc_csr));
+  for (int l = 0; l <= n_level; ++l) csr_copy(&A[l], &h->A[l]);
+  for (int l = 0; l < n_level; ++l) csr_copy(&P[l], &h->P[l]);
+  const orc_csr *c = &h->A[n_level];
+  h->n_coarse = c->m;
+  if (most_project_full) {
+    h->coarse_inv = (double *)calloc(c->m * c->m ? c->m * c->m : 1, sizeof(double));
+    for (int64_t i = 0; i < c->m; ++i)
+      for (int64_t q = c->rowptr[i]; q < c->rowptr[i + 1]; ++q) h->coarse_inv[i * c->m + c->cols[q]] = c->vals[q];
+    if (dense_inverse(c->m, h->coarse_inv)) return -1;
+  }
+  return 0;
+}
+
+int orc_lazy_project(const orc_csr *M, orc_csr *P, orc_csr *Pt) {
+  const int64_t m = M->m;
+  const int64_t *rs = M->rowptr, *cn = M->cols;
+  int64_t *counter = (int64_t *)calloc(m ? m : 1, sizeof(int64_t));
+  int64_t *core = (int64_t *)malloc(sizeof(int64_t) * (m ? m : 1));
+  int64_t nc = 0;
+  for (int64_t i = 0; i < m; ++i) {
+    if (counter[i] > 0) continue;
+    for (int64_t j = rs[i] + 1; j < rs[i + 1]; ++j) counter[cn[j]]++;
+    core[nc++] = i;
+  }
+  /* SparsityPattern::max_entries_per_row() of a compressed pattern: rows 1..m-1 */
+  int64_t cap = 0;
+  for (int64_t i = 1; i < m; ++i) cap = (rs[i] - rs[i - 1]) > cap ? (rs[i] - rs[i - 1]) : cap;
+  const int square = (nc == m);
+  int64_t *ps = (int64_t *)malloc(sizeof(int64_t) * (nc + 1));
+  int64_t *ts = (int64_t *)malloc(sizeof(int64_t) * (m + 1));
+  for (int64_t i = 0; i <= nc; ++i) ps[i] = i * cap;
+  for (int64_t i = 0; i <= m; ++i) ts[i] = i * cap;
+  int64_t *pslots = (int64_t *)malloc(sizeof(int64_t) * (nc * cap ? nc * cap : 1));
+  int64_t *tslots = (int64_t *)malloc(sizeof(int64_t) * (m * cap ? m * cap : 1));
+  for (int64_t k = 0; k < nc * cap; ++k) pslots[k] = INVALID;
+  for (int64_t k = 0; k < m * cap; ++k) tslots[k] = INVALID;
+  if (square && cap > 0) {
+    for (int64_t i = 0; i < nc; ++i) pslots[i * cap] = i;
+    for (int64_t i = 0; i < m; ++i) tslots[i * cap] = i;
+  }
+  for (int64_t i = 0; i < nc; ++i) {
+    const int64_t k = core[i];
+    pattern_add(pslots, ps[i], ps[i + 1], k);
+    pattern_add(tslots, ts[k], ts[k + 1], i);
+    for (int64_t j = rs[k] + 1; j < rs[k + 1]; ++j) {
+      pattern_add(pslots, ps[i], ps[i + 1], cn[j]);
+      pattern_add(tslots, ts[cn[j]], ts[cn[j] + 1], i);
+    }
+  }
+  P->m = nc; P->n = m;
+  Pt->m = m; Pt->n = nc;
+  pattern_compress(nc, square, ps, pslots, P);
+  pattern_compress(m, square, ts, tslots, Pt);
+  for (int64_t i = 0; i < nc; ++i) {
+    const int64_t k = core[i];
+    matrix_add(P, i, k, 1.0);
+    matrix_add(Pt, k, i, 1.0);
+    for (int64_t j = rs[k] + 1; j < rs[k + 1]; ++j) {
+      const int64_t l = cn[j];
+      matrix_add(P, i, l, 1.0 / counter[l]);
+      matrix_add(Pt, l, i, 1.0 / counter[l]);
+    }
+  }
+  free(counter); free(core); free(ps); free(ts); free(pslots); free(tslots);
+  return 0;
+}
+
+static int coarse_inverse(orc_amg *h) {
+  const orc_csr *c = &h->A[h->n_level];
+  h->n_coarse = c->m;
+  free(h->coarse_inv);
+  h->coarse_inv = NULL;
+  if (!h->most_project_full) return 0;
+  h->coarse_inv = (double *)calloc(c->m * c->m ? c->m * c->m : 1, sizeof(double));
+  for (int64_t i = 0; i < c->m; ++i)
+    for (int64_t q = c->rowptr[i]; q < c->rowptr[i + 1]; ++q) h->coarse_inv[i * c->m + c->cols[q]] = c->vals[q];
+  return dense_inverse(c->m, h->coarse_inv);
+}
+
+int orc_amg_setup_lazy(const orc_csr *a, int smooth_step, int64_t max_coarse, double min_density, orc_amg *h) {
+  memset(h, 0, sizeof(*h));
+  h->smooth_step = smooth_step;
+  h->alpha = 0.25;
+  int cap = 8;
+  h->A = (orc_csr *)calloc(cap + 1, sizeof(orc_csr));
+  h->P = (orc_csr *)calloc(cap, sizeof(orc_csr));
+  h->Pt = (orc_csr *)calloc(cap, sizeof(orc_csr));
+  csr_copy(a, &h->A[0]);
+  uint64_t k = (uint64_t)a->m, m = k;
+  float sparse_degree = (float)a->rowptr[a->m] / ((float)m * m);
+  h->most_project_full = 1;
+  while (m > (uint64_t)max_coarse || sparse_degree < min_density) {
+    orc_csr P, Pt, Ac;
+    orc_lazy_project(&h->A[h->n_level], &P, &Pt);
+    rap_with_pt(&P, &h->A[h->n_level], &Pt, &Ac);
+    m = (uint64_t)Ac.m;
+    if (k == m) {
+      h->most_project_full = 0;
+      orc_csr_free(&P); orc_csr_free(&Pt); orc_csr_free(&Ac);
+      break;
+    }
+    k = m;
+    if (h->n_level == cap) {
+      cap *= 2;
+      h->A = (orc_csr *)realloc(h->A, sizeof(orc_csr) * (cap + 1));
+      h->P = (orc_csr *)realloc(h->P, sizeof(orc_csr) * cap);
+      h->Pt = (orc_csr *)realloc(h->Pt, sizeof(orc_csr) * cap);
+    }
+    h->P[h->n_level] = P;
+    h->Pt[h->n_level] = Pt;
+    h->A[h->n_level + 1] = Ac;
+    sparse_degree = (float)Ac.rowptr[Ac.m] / ((float)m * m);
+    h->n_level++;
+  }
+  return coarse_inverse(h);
+}
+
+int orc_amg_lazy_reinit(orc_amg *h, const orc_csr *a) {
+  if (h->Pt == NULL) return -1;
+  orc_csr_free(&h->A[0]);
+  csr_copy(a, &h->A[0]);
+  for (int l = 0; l < h->n_level; ++l) {
+    orc_csr Ac;
+    rap_with_pt(&h->P[l], &h->A[l], &h->Pt[l], &Ac);
+    orc_csr_free(&h->A[l + 1]);
+    h->A[l + 1] = Ac;
+  }
+  return coarse_inverse(h);
+}
+
 void orc_amg_free(orc_amg *h) {
   for (int l = 0; l <= h->n_level; ++l) orc_csr_free(&h->A[l]);
   for (int l = 0; l < h->n_level; ++l) orc_csr_free(&h->P[l]);
+  if (h->Pt) {
+    for (int l = 0; l < h->n_level; ++l) orc_csr_free(&h->Pt[l]);
+    free(h->Pt);
+  }
   free(h->A);
   free(h->P);
   free(h->coarse_inv);

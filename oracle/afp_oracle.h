@@ -57,10 +57,25 @@ typedef struct {
   double *coarse_inv;   /* explicit inverse of A[n_level], row-major */
   int smooth_step;
   double alpha;
+  orc_csr *Pt;          /* lazy hierarchy only: lazyProject's own P^T per level */
 } orc_amg;
+
+/* lazyProject (src/AMGSolver.cpp:235-284) */
+int orc_lazy_project(const orc_csr *m, orc_csr *p, orc_csr *pt);
+/* lazyInit (src/AMGSolver.cpp:442-503) */
+int orc_amg_setup_lazy(const orc_csr *a, int smooth_step, int64_t max_coarse, double min_density, orc_amg *out);
+/* lazyReinit on an initialised lazy hierarchy (src/AMGSolver.cpp:505-545):
+ * recomputes every level from a (same pattern) with the stored P, Pt. */
+int orc_amg_lazy_reinit(orc_amg *h, const orc_csr *a);
 
 int orc_amg_setup(const orc_csr *a, int smooth_step, int64_t max_coarse, double min_density,
                   double alpha, orc_amg *out);
+/* A hierarchy from given level matrices A[0..n_level] and projections
+ * P[0..n_level-1] (copied); the coarsest inverse is computed here when
+ * most_project_full.  Used to time the reference's solve phase on a
+ * hierarchy that was built (and checked equal to the reference's) elsewhere. */
+int orc_amg_from_levels(int n_level, const orc_csr *A, const orc_csr *P, int most_project_full,
+                        int smooth_step, orc_amg *out);
 void orc_amg_free(orc_amg *h);
 /* Project() alone: C/F split and projection P for one level.
  * cf_out[i] = -1 for C-points, 1 for F-points (may be NULL). */

@@ -26,7 +26,7 @@ class _CSR(C.Structure):
 class _AMG(C.Structure):
     _fields_ = [("n_level", C.c_int), ("most_project_full", C.c_int), ("A", C.POINTER(_CSR)),
                 ("P", C.POINTER(_CSR)), ("n_coarse", C.c_int64), ("coarse_inv", _f64p),
-                ("smooth_step", C.c_int), ("alpha", C.c_double)]
+                ("smooth_step", C.c_int), ("alpha", C.c_double), ("Pt", C.POINTER(_CSR))]
 
 
 def build() -> str:
@@ -34,7 +34,9 @@ def build() -> str:
     src = os.path.join(HERE, "afp_oracle.c")
     if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
             os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "afp_oracle.h"))):
-        subprocess.check_call(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-o", LIB_PATH, src, "-lm"])
+        base = ["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-o", LIB_PATH, src, "-lm"]
+        if subprocess.run(base + ["-fopenmp"], capture_output=True).returncode != 0:
+            subprocess.check_call(base)  # serial build where OpenMP is unavailable
     return LIB_PATH
 
 
@@ -52,12 +54,16 @@ def lib():
         _lib.orc_amg_setup.argtypes = [C.POINTER(_CSR), C.c_int, C.c_int64, C.c_double, C.c_double,
                                        C.POINTER(_AMG)]
         _lib.orc_amg_free.argtypes = [C.POINTER(_AMG)]
+        _lib.orc_amg_from_levels.argtypes = [C.c_int, C.POINTER(_CSR), C.POINTER(_CSR), C.c_int, C.c_int,
+                                             C.POINTER(_AMG)]
         _lib.orc_project.argtypes = [C.POINTER(_CSR), C.c_double, C.POINTER(_CSR), _i32p]
         _lib.orc_rap.argtypes = [C.POINTER(_CSR), C.POINTER(_CSR), C.POINTER(_CSR)]
         _lib.orc_amg_vcycles.argtypes = [C.POINTER(_AMG), _f64p, _f64p, C.c_int]
         _lib.orc_pcg.argtypes = [C.POINTER(_CSR), C.POINTER(_AMG), _f64p, _f64p, C.c_double, C.c_int, _f64p]
         _lib.orc_pcg.restype = C.c_int
         _lib.orc_csr_free.argtypes = [C.POINTER(_CSR)]
+        _lib.orc_amg_setup_lazy.argtypes = [C.POINTER(_CSR), C.c_int, C.c_int64, C.c_double, C.POINTER(_AMG)]
+        _lib.orc_amg_lazy_reinit.argtypes = [C.POINTER(_AMG), C.POINTER(_CSR)]
     return _lib
 
 
@@ -166,6 +172,35 @@ class AMG:
         rc = lib().orc_amg_setup(C.byref(A._c()), smooth_step, max_coarse, min_density, alpha, C.byref(self._h))
         if rc != 0:
             raise RuntimeError("orc_amg_setup failed (singular coarsest matrix)")
+
+    @classmethod
+    def lazy(cls, A: CSR, smooth_step=3, max_coarse=50, min_density=0.382):
+        """lazyInit: the hierarchy AMGPreconditioner builds."""
+        self = cls.__new__(cls)
+        self._A = A
+        self._h = _AMG()
+        if lib().orc_amg_setup_lazy(C.byref(A._c()), smooth_step, max_coarse, min_density, C.byref(self._h)):
+            raise RuntimeError("singular coarsest matrix")
+        return self
+
+    def lazy_reinit(self, A: CSR):
+        self._A = A
+        if lib().orc_amg_lazy_reinit(C.byref(self._h), C.byref(A._c())):
+            raise RuntimeError("lazy re-setup failed")
+
+    @classmethod
+    def from_levels(cls, A_levels, P_levels, most_project_full=True, smooth_step=3):
+        """A hierarchy built elsewhere: A_levels[0..L], P_levels[0..L-1] (CSR)."""
+        self = cls.__new__(cls)
+        self._A = A_levels[0]
+        L = len(P_levels)
+        As = (_CSR * (L + 1))(*[a._c() for a in A_levels])
+        Ps = (_CSR * max(L, 1))(*[p._c() for p in P_levels]) if L else (_CSR * 1)()
+        self._h = _AMG()
+        rc = lib().orc_amg_from_levels(L, As, Ps, int(most_project_full), smooth_step, C.byref(self._h))
+        if rc != 0:
+            raise RuntimeError("singular coarsest matrix")
+        return self
 
     def __del__(self):
         if getattr(self, "_h", None) is not None and lib is not None:

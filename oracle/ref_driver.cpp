@@ -282,6 +282,27 @@ int run() {
          << ", \"pcg_relres\": " << rel;
     }
   }
+  if (arg("lazy", "0") == "1") {
+    // AMGPreconditioner: lazyReinit -> lazyInit, vmult = iterate_step+1 V-cycles,
+    // then a numeric re-setup for new values on the same pattern object.
+    const int smooth = std::atoi(arg("smooth", "3").c_str());
+    AMGPreconditioner pre(A, 2, smooth);
+    js << ", \"lazy_n_project\": " << pre.n_project;
+    for (u_int l = 0; l < pre.n_project; ++l) {
+      dump_csr(out, "LP" + std::to_string(l), *pre.project_matrix[l]);
+      dump_csr(out, "LPt" + std::to_string(l), *pre.project_matrix_r[l]);
+      dump_csr(out, "LA" + std::to_string(l + 1), *pre.projected_matrix[l + 1]);
+    }
+    Vector<double> x(n);
+    pre.vmult(x, b);
+    save_npy(out + "/x_lazy.npy", &x(0), {n});
+    for (size_t k = 0; k < A.n_nonzero_elements(); ++k) A.global_entry(k) *= 1.5;
+    pre.reinit(A, 2);
+    for (u_int l = 0; l < pre.n_project; ++l) dump_csr(out, "LRA" + std::to_string(l + 1), *pre.projected_matrix[l + 1]);
+    Vector<double> x2(n);
+    pre.vmult(x2, b);
+    save_npy(out + "/x_lazy2.npy", &x2(0), {n});
+  }
   js << "}";
   std::cout << js.str() << std::endl;
   return 0;

@@ -56,7 +56,7 @@ def make(name, spec):
         f.tofile(os.path.join(d, "f.bin"))
         args = [DRIVER, f"mesh={d}/m.mesh", f"dim={mesh.dim}", f"deg={deg}", f"out={d}", f"f={d}/f.bin",
                 f"acc_stiff={acc_s}", f"acc_mass={acc_m}", "amg=1", f"dump_levels={int(levels)}", "vcycles=2",
-                "pcg_tol=1e-10"]
+                "pcg_tol=1e-10", "lazy=1"]
         if coef is not None:
             coef.tofile(os.path.join(d, "coef.bin"))
             args.append(f"coef={d}/coef.bin")
@@ -76,6 +76,14 @@ def make(name, spec):
         for l in range(meta["n_project"]):
             out.update(load_csr(d, f"P{l}"))
             out.update(load_csr(d, f"A{l + 1}"))
+        out["lazy_n_project"] = meta["lazy_n_project"]
+        out["x_lazy"] = np.load(os.path.join(d, "x_lazy.npy"))
+        out["x_lazy2"] = np.load(os.path.join(d, "x_lazy2.npy"))
+        for l in range(meta["lazy_n_project"]):
+            out.update(load_csr(d, f"LP{l}"))
+            out.update(load_csr(d, f"LPt{l}"))
+            out.update(load_csr(d, f"LA{l + 1}"))
+            out.update(load_csr(d, f"LRA{l + 1}"))
         inv = os.path.join(d, "coarse_inverse.npy")
         if os.path.exists(inv):
             out["coarse_inverse"] = np.load(inv)

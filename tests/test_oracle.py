@@ -48,3 +48,25 @@ def test_dirichlet_and_hierarchy_bitwise(name):
     x, it, rel = amg.pcg(b, 1e-10)
     assert rel <= 1e-10 and abs(it - int(g["pcg_iters"])) <= 1
     assert np.abs(x - g["x_pcg"]).max() <= 1e-9 * np.abs(g["x_pcg"]).max()
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_lazy_hierarchy_bitwise(name):
+    """lazyInit / lazyReinit (AMGPreconditioner) restated against the reference."""
+    g = load_golden(name)
+    S = golden_csr(g, "system")
+    amg = O.AMG.lazy(S)
+    assert amg.n_level == int(g["lazy_n_project"])
+    for l in range(amg.n_level):
+        for mine, ref in ((amg.projection(l), golden_csr(g, f"LP{l}")), (amg.level(l + 1), golden_csr(g, f"LA{l + 1}"))):
+            assert np.array_equal(mine.rowptr, ref.rowptr) and np.array_equal(mine.cols, ref.cols)
+            assert np.array_equal(mine.vals, ref.vals)
+    x = amg.vcycles(np.zeros_like(g["rhs"]), g["rhs"], 3)  # vmult with iterate_step 2
+    assert np.allclose(x, g["x_lazy"], rtol=1e-11, atol=1e-13 * np.abs(g["x_lazy"]).max())
+    S2 = O.CSR(S.rowptr, S.cols, S.vals * 1.5, S.shape)
+    amg.lazy_reinit(S2)
+    for l in range(amg.n_level):
+        ref = golden_csr(g, f"LRA{l + 1}")
+        assert np.array_equal(amg.level(l + 1).vals, ref.vals)
+    x2 = amg.vcycles(np.zeros_like(g["rhs"]), g["rhs"], 3)
+    assert np.allclose(x2, g["x_lazy2"], rtol=1e-11, atol=1e-13 * np.abs(g["x_lazy2"]).max())
