@@ -46,6 +46,36 @@ class SolveInfo(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("workers", C.c_int), ("hbm_budget_bytes", C.c_int64), ("precision", C.c_int), ("tol", C.c_double),
+                ("maxit", C.c_int), ("dense_tail", C.c_int)]
+
+
+class Request(C.Structure):
+    _fields_ = [("dim", C.c_int), ("degree", C.c_int), ("acc_stiff", C.c_int), ("acc_mass", C.c_int),
+                ("n_vertex", C.c_int64), ("coords", C.c_void_p), ("n_cell", C.c_int64), ("cells", C.c_void_p),
+                ("n_dof", C.c_int64), ("elem_dof", C.c_void_p), ("dirichlet", C.c_void_p), ("coef", C.c_void_p),
+                ("f", C.c_void_p)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("rel_residual", C.c_double),
+                ("queue_seconds", C.c_double), ("setup_seconds", C.c_double), ("latency_seconds", C.c_double),
+                ("device_seconds", C.c_double), ("estimate_bytes", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64), ("p50_seconds", C.c_double),
+                ("p99_seconds", C.c_double), ("solves_per_second", C.c_double), ("budget_bytes", C.c_int64),
+                ("in_use_bytes", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # (name, argtypes) of every exported entry point; the restype is afp_status
 # (c_int) unless noted in _RESTYPES.
 SIGNATURES = {
@@ -86,9 +116,17 @@ SIGNATURES = {
     "afp_host_coarsen": [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, c_i64p,
                          C.POINTER(c_i32p), C.POINTER(c_i32p), C.POINTER(c_f64p)],
     "afp_host_free": [C.c_void_p],
+    "afp_server_default_opts": [C.POINTER(ServerOpts)],
+    "afp_server_create": [C.c_int, C.POINTER(ServerOpts), c_void_pp],
+    "afp_server_submit": [C.c_void_p, C.POINTER(Request), c_i64p],
+    "afp_server_wait": [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(RequestResult)],
+    "afp_server_poll": [C.c_void_p, C.c_int64, C.POINTER(C.c_int)],
+    "afp_server_get_stats": [C.c_void_p, C.POINTER(ServerStats)],
+    "afp_server_reset_stats": [C.c_void_p],
+    "afp_server_destroy": [C.c_void_p],
 }
 _RESTYPES = {"afp_version": C.c_int, "afp_status_string": C.c_char_p, "afp_last_error": C.c_char_p,
-             "afp_amg_default_opts": None, "afp_host_free": None}
+             "afp_amg_default_opts": None, "afp_host_free": None, "afp_server_default_opts": None}
 
 _lib = None
 

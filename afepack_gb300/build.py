@@ -29,6 +29,7 @@ SOURCES = [
     ("amg.cu", []),
     ("mrhs.cu", []),
     ("coarsen_host.cpp", []),
+    ("server.cpp", []),
 ]
 HEADERS = ["common.cuh", "kernels.cuh", "solve.cuh", "amg_internal.cuh", "quadrature_tables.h"]
 

@@ -202,6 +202,69 @@ afp_status afp_pcg_solve(afp_amg *amg, double *x, const double *b, double tol, i
 afp_status afp_pcg_solve_multi(afp_amg *amg, double *X, const double *B, int nrhs, double tol,
                                int maxit, afp_solve_info *info);
 
+/* -------------------------------------------------------------- serving */
+/* A solve server: continuous batching of independent requests on one GPU
+ * (no counterpart in the reference, which solves one system per call).  Each
+ * request carries its own mesh and data and runs the whole path --
+ * afp_space_create, afp_assemble, b = M f, afp_apply_dirichlet (zero data),
+ * afp_amg_setup, afp_pcg_solve -- in one of `workers` execution slots, each
+ * with its own stream, so admitted requests overlap on the device and their
+ * host C/F work runs in parallel.  A request is admitted, in arrival order,
+ * when a slot is free and its estimated device footprint fits the budget. */
+typedef struct afp_server afp_server;
+
+typedef struct afp_server_opts {
+  int workers;                 /* execution slots (default 8)                   */
+  int64_t hbm_budget_bytes;    /* admission budget; 0 = 80% of free memory      */
+  int precision;               /* afp_precision of the V-cycle (default MIXED)  */
+  double tol;                  /* relative residual of the CG (default 1e-10)   */
+  int maxit;                   /* CG iteration limit (default 500)              */
+  int dense_tail;              /* afp_amg_opts.dense_tail, -1 = its default      */
+} afp_server_opts;
+
+typedef struct afp_request {
+  int dim, degree, acc_stiff, acc_mass;
+  int64_t n_vertex;
+  const double *coords;        /* [n_vertex*dim]                                */
+  int64_t n_cell;
+  const int32_t *cells;        /* [n_cell*(dim+1)]                              */
+  int64_t n_dof;
+  const int32_t *elem_dof;     /* [n_cell*nd]                                   */
+  const int32_t *dirichlet;    /* [n_dof] nonzero on Dirichlet DOFs (zero data) */
+  const double *coef;          /* [n_cell] coefficient or NULL                   */
+  const double *f;             /* [n_dof] nodal data, b = M f                    */
+} afp_request;                 /* host arrays; copied by afp_server_submit       */
+
+typedef struct afp_request_result {
+  int status;                  /* afp_status of the request                     */
+  int iterations;
+  double rel_residual;
+  double queue_seconds;        /* submit -> admission                           */
+  double setup_seconds;        /* admission -> hierarchy ready                  */
+  double latency_seconds;      /* submit -> solution ready                      */
+  double device_seconds;       /* device time of the CG                         */
+  int64_t estimate_bytes;      /* admitted footprint                            */
+} afp_request_result;
+
+typedef struct afp_server_stats {
+  int64_t completed, failed, queued;
+  double p50_seconds, p99_seconds;   /* latency percentiles of completed requests */
+  double solves_per_second;          /* completed / (last completion - stats start) */
+  int64_t budget_bytes, in_use_bytes;
+} afp_server_stats;
+
+void afp_server_default_opts(afp_server_opts *opts);
+afp_status afp_server_create(int device, const afp_server_opts *opts, afp_server **out);
+afp_status afp_server_submit(afp_server *s, const afp_request *req, int64_t *ticket);
+/* Blocks until the request is done; copies its solution (n_dof doubles) to x
+ * when x != NULL and releases the ticket. */
+afp_status afp_server_wait(afp_server *s, int64_t ticket, double *x, afp_request_result *res);
+afp_status afp_server_poll(afp_server *s, int64_t ticket, int *done);
+afp_status afp_server_get_stats(afp_server *s, afp_server_stats *stats);
+afp_status afp_server_reset_stats(afp_server *s);
+/* Finishes queued requests, then stops the slots. */
+afp_status afp_server_destroy(afp_server *s);
+
 /* ----------------------------------------------------------- host logic */
 /* The C/F splitting and projection of one level (Project, src/AMGSolver.cpp:18-226),
  * run on the host on a host CSR; no GPU needed.  cf receives -1 for C and 1
