@@ -30,7 +30,7 @@ def default_opts() -> N.AMGOpts:
 class AMGSolver:
     def __init__(self, M: SparseMatrix | None = None, tol: float = 1.0e-12, s: int = 3, nmpo: int = 50,
                  nmpsd: float = 0.382, alp: float = 0.25, *, precision: int = FP64, dense_tail: int | None = None,
-                 max_colors: int | None = None, symmetric: bool = True):
+                 max_colors: int | None = None, symmetric: bool = True, coarse_colors: int | None = None):
         self.opts = default_opts()
         self.opts.tolerance = tol
         self.opts.smooth_step = s
@@ -43,6 +43,8 @@ class AMGSolver:
         if max_colors is not None:
             self.opts.max_colors = max_colors
         self.opts.symmetric = int(symmetric)
+        if coarse_colors is not None:
+            self.opts.coarse_colors = coarse_colors
         self.handle = None
         self.matrix = None
         if M is not None:

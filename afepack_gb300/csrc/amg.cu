@@ -230,13 +230,14 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
     L.nnz = H.nnz();
     if (l < t) {
       std::vector<int> color;
-      int K = host_color(H, h->opts.max_colors, color);
+      const int cap = (l > 0 && h->opts.coarse_colors > 0) ? h->opts.coarse_colors : h->opts.max_colors;
+      int K = host_color(H, cap, color);
       const int nclass = K;
       std::vector<int64_t> cnt(nclass + 1, 0);
       for (int64_t i = 0; i < n; ++i) cnt[color[i] + 1]++;
       for (int c = 0; c < nclass; ++c) cnt[c + 1] += cnt[c];
       L.cls.assign(cnt.begin(), cnt.end());
-      L.overflow = (K == h->opts.max_colors + 1);
+      L.overflow = (K == cap + 1);
       std::vector<int64_t> cur(cnt.begin(), cnt.end() - 1);
       for (int64_t i = 0; i < n; ++i) perm[l][cur[color[i]]++] = (int)i;
     } else {
@@ -546,6 +547,7 @@ void afp_amg_default_opts(afp_amg_opts* o) {
   o->dense_tail = 1024;
   o->max_colors = 32;
   o->symmetric = 1;
+  o->coarse_colors = 8;
 }
 
 afp_status afp_amg_setup(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out) {

@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="poisson3d_p1_64", choices=sorted(WORKLOADS))
     ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--stream", action="store_true", help="served request stream instead of one workload")
+    ap.add_argument("--stream-sample", type=int, default=48)
+    ap.add_argument("--workers", type=int, default=8)
     return ap.parse_args()
 
 
@@ -236,6 +239,10 @@ def run_ours(args):
             "traffic": None, "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"}
 
     launches = ctx.launch_count()
+    # CPU baseline (rank 0, N=1): the reference algorithm's solve on one core
+    amg_full = AMGSolver(K, precision=FP64, dense_tail=0)
+    cpu = cpu_baseline_sample(amg_full, b.cpu().numpy().copy(), args.tol)
+    del amg_full
     line = {
         "metric": METRIC, "value": round(results["mixed"]["solves_per_s"], 3), "unit": "solves/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -251,13 +258,155 @@ def run_ours(args):
         "e2e": {"value": round(1e3 * len(e2e_t) / e2e_t.sum(), 3), "unit": "solves/s",
                 "h2d_bytes_per_step": int(bh.numel() * 8), "d2h_bytes_per_step": int(xh.numel() * 8),
                 "p50_ms": round(float(np.percentile(e2e_t, 50)), 3), "p99_ms": round(float(np.percentile(e2e_t, 99)), 3)},
-        "roofline": roof, "clocks": clk, "gpu_launches": int(launches),
+        "roofline": roof, "clocks": clk, "gpu_launches": int(launches), "cpu_baseline": cpu,
     }
     return line
 
 
+def run_stream(args):
+    """Served stream (independent 2D P1 requests, n log-uniform in [32,1024],
+    half variable-coefficient): a bounded sample of the stream is submitted at
+    once (saturation) to the solve server, mixed precision and FP64."""
+    from afepack_gb300 import workloads as W
+    from afepack_gb300 import build as B
+    from afepack_gb300.serve import Server
+    B.build()
+    reqs = W.request_stream(2000, seed=4)[: args.stream_sample]
+    t0 = time.perf_counter()
+    wls = [W.request_workload(r) for r in reqs]
+    gen_s = time.perf_counter() - t0
+    out = {}
+    for name, prec in (("mixed", 1), ("fp64", 0)):
+        with Server(workers=args.workers, precision=prec, tol=args.tol) as srv:
+            warm = [srv.submit(wl) for wl in wls[: min(4, len(wls))]]
+            for t in warm:
+                srv.wait(t)
+            srv.reset_stats()
+            s0 = time.perf_counter()
+            tickets = [srv.submit(wl) for wl in wls]
+            res = [srv.wait(t)[1] for t in tickets]
+            wall = time.perf_counter() - s0
+            st = srv.stats()
+        lat = np.array([r["latency_seconds"] for r in res])
+        out[name] = {"solves_per_s": len(res) / wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                     "p99_ms": 1e3 * float(np.percentile(lat, 99)), "failed": int(st["failed"]),
+                     "iterations_median": int(np.median([r["iterations"] for r in res]))}
+    ndofs = [int(w.space.n_dof) for w in wls]
+    return {
+        "metric": METRIC, "value": round(out["mixed"]["solves_per_s"], 3), "unit": "solves/s", "n_gpus": 1,
+        "steps": 1, "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 V-cycle (bf16 P/P^T) + fp64 CG", "data": "synthetic (seeded)",
+        "config": {"workload": "request_stream", "requests": len(wls), "workers": args.workers,
+                   "n_dof_min": min(ndofs), "n_dof_max": max(ndofs), "n_dof_total": sum(ndofs), "tol": args.tol,
+                   "arrival": "all at once (saturation)", "generation_s": round(gen_s, 2)},
+        "p50_ms": round(out["mixed"]["p50_ms"], 2), "p99_ms": round(out["mixed"]["p99_ms"], 2),
+        "fp64": out["fp64"], "mixed": out["mixed"],
+        "mixed_over_fp64": round(out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"], 3),
+    }
+
+
+def _oracle_system(wl):
+    """The workload's system built by the CPU oracle (the reference algorithm):
+    assembly, b = M f, Dirichlet elimination."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    K, mass = O.assemble(wl.space, wl.acc_stiff, wl.acc_mass, wl.coef)
+    b = O.CSR(K.rowptr, K.cols, mass, K.shape).matvec(wl.f)
+    O.apply_dirichlet(K, b, wl.space.dof_bmark)
+    return K, b
+
+
+def _ref_worker(conn, steps, warmup, tol):
+    """Forked reference worker: times single-threaded oracle CG solves
+    (one reference V-cycle per iteration) on the hierarchy of its parent."""
+    import oracle as O  # noqa: F401  (already loaded in the parent)
+    amg, b = _REF_STATE["amg"], _REF_STATE["b"]
+    for i in range(warmup + steps):
+        conn.recv()  # start signal for this step
+        t0 = time.perf_counter()
+        x, it, rel = amg.pcg(b, tol, 1000)
+        conn.send((time.perf_counter() - t0, it, rel))
+    conn.close()
+
+
+_REF_STATE = {}
+
+
 def run_reference(args):
-    return {"impl": "reference", "unavailable": "reference arm not wired yet"}
+    """The reference's CPU implementation of the path, timed on the host cores:
+    the oracle port of AFEPack (bit-identical to AFEPack compiled from its
+    sources on every fixture) builds the system and hierarchy once, then W
+    forked single-threaded processes (W = host cores) each run one CG solve
+    per step; value = W / (wall time of the step)."""
+    import multiprocessing as mp
+    from afepack_gb300 import workloads as W
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    wl = WORKLOADS[args.workload](W)
+    t0 = time.perf_counter()
+    K, b = _oracle_system(wl)
+    t1 = time.perf_counter()
+    amg = O.AMG(K)  # AMGSolver::reinit restated (rows of the Galerkin product on all cores)
+    t2 = time.perf_counter()
+    _REF_STATE.update(amg=amg, b=b)
+    ctx = mp.get_context("fork")  # no GPU is touched in this process
+    pipes, procs = [], []
+    for _ in range(cores):
+        a, c = ctx.Pipe()
+        p = ctx.Process(target=_ref_worker, args=(c, args.steps, args.warmup, args.tol))
+        p.start()
+        pipes.append(a)
+        procs.append(p)
+    os.environ["OMP_NUM_THREADS"] = "1"
+    walls, iters = [], []
+    for i in range(args.warmup + args.steps):
+        s0 = time.perf_counter()
+        for a in pipes:
+            a.send(i)
+        res = [a.recv() for a in pipes]
+        wall = time.perf_counter() - s0
+        if i >= args.warmup:
+            walls.append(wall)
+            iters.append(res[0][1])
+    for p in procs:
+        p.join()
+    walls = np.array(walls)
+    value = cores * len(walls) / walls.sum()
+    n0 = K.shape[0]
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * walls.mean(), 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "n_dof": int(n0), "nnz": int(K.nnz), "tol": args.tol,
+                   "levels": [list(map(int, (amg.level(l).shape[0], amg.level(l).nnz))) for l in range(amg.n_level + 1)],
+                   "parallelism": f"{cores} single-threaded processes, one solve each per step"},
+        "pcg_iterations": int(np.median(iters)),
+        "setup": {"assembly_dirichlet_s": round(t1 - t0, 2), "amg_reinit_s": round(t2 - t1, 2),
+                  "amg_reinit_threads": cores},
+        "cpu_baseline": {"value": round(value, 4), "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} concurrent CG solves (one reference V-cycle per iteration) per step"},
+        "e2e": {"value": round(value, 4), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def cpu_baseline_sample(amg_gpu, b_host, tol):
+    """One single-threaded oracle CG solve on the hierarchy the GPU built at the
+    reference's full depth (bitwise the reference's, which the tests check)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    nl = amg_gpu.n_project()
+    A = [O.CSR(*amg_gpu.level_matrix(l), (amg_gpu.level_info(l)[0],) * 2) for l in range(nl + 1)]
+    P = [O.CSR(*amg_gpu.projection(l), (amg_gpu.level_info(l + 1)[0], amg_gpu.level_info(l)[0])) for l in range(nl)]
+    amg = O.AMG.from_levels(A, P)
+    t0 = time.perf_counter()
+    x, it, rel = amg.pcg(b_host, tol, 1000)
+    dt = time.perf_counter() - t0
+    return {"value": round(1.0 / dt, 4), "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": f"one CG solve of the same system ({it} iterations, one reference V-cycle each) on 1 core; "
+                      f"hierarchy levels bitwise the reference's"}
 
 
 def main():
@@ -267,7 +416,7 @@ def main():
         if rank == 0:
             print(json.dumps(run_reference(args)))
         return
-    line = run_ours(args)
+    line = run_stream(args) if args.stream else run_ours(args)
     if rank == 0:
         print(json.dumps(line))
 

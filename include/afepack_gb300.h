@@ -138,6 +138,9 @@ typedef struct afp_amg_opts {
                            an l1-Jacobi overflow class (default 32)             */
   int symmetric;        /* post-smoothing visits colours in reverse order so the
                            V-cycle is a symmetric preconditioner (default 1)    */
+  int coarse_colors;    /* colour-class cap on levels >= 1 (default 8; 0 = use
+                           max_colors); their long rows would otherwise need
+                           dozens of sequential classes                         */
 } afp_amg_opts;
 
 typedef struct afp_solve_info {

@@ -1,0 +1,54 @@
+"""The C++ drop-in (afepack_gb300/dropin/AMGSolver_gb300.cpp) compiles against
+AFEPack's unchanged AMGSolver.h and links with the rest of AFEPack and
+libafepack_gb300.so in place of src/AMGSolver.cpp.  Needs the reference
+sources (skipped where they are not mounted); nothing is run."""
+import glob
+import os
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+REF = "/root/reference"
+OBJ = os.path.join(ROOT, "oracle", "_ref", "obj")
+
+MAIN = r"""
+#include <AFEPack/AMGSolver.h>
+using namespace AFEPack;
+int main() {
+  SparsityPattern sp(1, 1, (size_t)1);
+  sp.compress();
+  SparseMatrix<double> A(sp);
+  AMGSolver solver;   // construct only: reinit/solve would need a GPU
+  Vector<double> x(1), r(1);
+  if (false) { solver.reinit(A); solver.solve(x, r, 1e-8, 200); }
+  return 0;
+}
+"""
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include")), reason="reference sources not mounted")
+def test_dropin_links_into_afepack(native, tmp_path):
+    if not os.path.exists(os.path.join(OBJ, "BilinearOperator.o")):
+        subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "-j8"],
+                              stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    flags = ["-std=c++20", "-O1", "-w", "-I" + os.path.join(ROOT, "oracle", "shim"), "-I" + os.path.join(REF, "include"),
+             "-I" + os.path.join(ROOT, "include")]
+    drop = tmp_path / "dropin.o"
+    subprocess.check_call(["g++", *flags, "-c", os.path.join(ROOT, "afepack_gb300", "dropin", "AMGSolver_gb300.cpp"),
+                           "-o", str(drop)])
+    main = tmp_path / "main.cpp"
+    main.write_text(MAIN)
+    objs = [o for o in glob.glob(os.path.join(OBJ, "*.o")) if not o.endswith(("AMGSolver.o", "ref_driver.o"))]
+    libdir = os.path.join(ROOT, "afepack_gb300", "_lib")
+    openblas = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-p", "-n"], capture_output=True,
+                              text=True).stdout
+    blas = [l.split(":=", 1)[1].strip() for l in openblas.splitlines() if l.startswith("OPENBLAS :=")]
+    blas_lib = [b for b in blas if b and os.path.exists(b)]
+    exe = tmp_path / "poisson_gpu"
+    cmd = ["g++", *flags, str(main), str(drop), *objs, *blas_lib, "-L" + libdir, "-lafepack_gb300",
+           "-Wl,-rpath," + libdir, "-ldl", "-pthread", "-o", str(exe)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr[-3000:]
+    assert exe.exists()
