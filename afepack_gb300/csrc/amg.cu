@@ -544,7 +544,7 @@ void afp_amg_default_opts(afp_amg_opts* o) {
   o->min_density = 0.382;
   o->alpha = 0.25;
   o->precision = AFP_PRECISION_FP64;
-  o->dense_tail = 1024;
+  o->dense_tail = 8192;
   o->max_colors = 32;
   o->symmetric = 1;
   o->coarse_colors = 8;
@@ -562,7 +562,7 @@ afp_status afp_amg_setup(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out)
     AFP_REQUIRE(o.smooth_step >= 0 && o.max_coarse >= 1 && o.alpha >= 0 && o.max_colors >= 1 && o.dense_tail >= 0 &&
                     (o.precision == AFP_PRECISION_FP64 || o.precision == AFP_PRECISION_MIXED),
                 AFP_ERR_INVALID, "invalid AMG options");
-    AFP_REQUIRE(o.dense_tail <= 8192, AFP_ERR_UNSUPPORTED, "dense_tail above 8192 rows");
+    AFP_REQUIRE(o.dense_tail <= 16384, AFP_ERR_UNSUPPORTED, "dense_tail above 16384 rows");
     setup(h.get(), a, false);
     *out = h.release();
   });

@@ -66,14 +66,16 @@ void host_project(const HostCSR& M, double alpha, std::vector<int>& flag, HostCS
     ++n_core;
   }
   // second pass: F points with a strong F-F connection lacking a common
-  // strong C neighbour become C points
-  std::vector<int> dep;
+  // strong C neighbour become C points.  The set of i's strong C neighbours
+  // is a marker array (dep_mark[c] == i) instead of the reference's list
+  // scan: the same membership answers in O(1), which keeps dense coarse
+  // levels (rows of ~10^3 entries) from turning the pass quadratic.
+  std::vector<int> dep_mark(m, -1);
   for (int i = 0; i < m; ++i) {
     if (flag[i] != 1) continue;
-    dep.clear();
     for (int j = rs[i] + 1; j < rs[i + 1]; ++j) {
       if (std::fabs(v[j]) < beta[i]) continue;
-      if (flag[cn[j]] == -1) dep.push_back(cn[j]);
+      if (flag[cn[j]] == -1) dep_mark[cn[j]] = i;
     }
     bool is_FF = false;
     for (int j = rs[i] + 1; j < rs[i + 1]; ++j) {
@@ -83,7 +85,7 @@ void host_project(const HostCSR& M, double alpha, std::vector<int>& flag, HostCS
       for (int j1 = rs[k] + 1; j1 < rs[k + 1]; ++j1) {
         const int k1 = cn[j1];
         if (flag[k1] != -1) continue;
-        if (std::find(dep.begin(), dep.end(), k1) != dep.end()) {
+        if (dep_mark[k1] == i) {
           is_FF = false;
           break;
         }

@@ -132,7 +132,7 @@ typedef struct afp_amg_opts {
   double alpha;         /* strong-connection threshold (default 0.25)           */
   int precision;        /* afp_precision of the V-cycle (default FP64)          */
   int dense_tail;       /* levels with at most this many rows are solved with a
-                           dense inverse instead of smoothed (default 1024;
+                           dense inverse instead of smoothed (default 8192;
                            0 keeps the reference depth)                         */
   int max_colors;       /* colour classes of the smoother before rows fall into
                            an l1-Jacobi overflow class (default 32)             */

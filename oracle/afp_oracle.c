@@ -227,10 +227,35 @@ static void pattern_compress(int64_t m, int square, const int64_t *slot_start, i
   out->rowptr[m] = pos;
 }
 
-/* SparseMatrix::add -- linear search of the row */
+/* position of column j in row i, -1 when absent.  Rows are [diagonal,
+ * ascending others] (square) or ascending (rectangular), so checking the
+ * first entry and binary-searching the rest finds what the reference's
+ * linear scans (SparseMatrix::add / el) find. */
+static int64_t row_find(const orc_csr *a, int64_t i, int64_t j) {
+  int64_t b = a->rowptr[i], e = a->rowptr[i + 1];
+  if (b == e) return -1;
+  if (a->cols[b] == j) return b;
+  int64_t lo = b + 1, hi = e;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) / 2;
+    if (a->cols[mid] < j) lo = mid + 1; else hi = mid;
+  }
+  return (lo < e && a->cols[lo] == j) ? lo : -1;
+}
+
+static int sorted_has(const int64_t *b, const int64_t *e, int64_t key) {
+  const int64_t *lo = b, *hi = e;
+  while (lo < hi) {
+    const int64_t *mid = lo + (hi - lo) / 2;
+    if (*mid < key) lo = mid + 1; else hi = mid;
+  }
+  return lo < e && *lo == key;
+}
+
+/* SparseMatrix::add: adds v to entry (i, j) when it is in the pattern */
 static void matrix_add(orc_csr *a, int64_t i, int64_t j, double v) {
-  for (int64_t k = a->rowptr[i]; k < a->rowptr[i + 1]; ++k)
-    if (a->cols[k] == j) { a->vals[k] += v; return; }
+  int64_t k = row_find(a, i, j);
+  if (k >= 0) a->vals[k] += v;
 }
 
 /* SparseMatrix::el -- 0 when (i,j) is not in the pattern */
@@ -472,12 +497,14 @@ static int project(const orc_csr *M, double alpha, orc_csr *P, orc_csr *Pt, int3
     flag[i] = -1;
     n_core++;
   }
+  /* dep[c] == i marks the strong C neighbours of F point i (the reference
+   * keeps them in a std::list and searches it; membership is the same) */
+  for (int64_t i = 0; i < m; ++i) dep[i] = -1;
   for (int64_t i = 0; i < m; ++i) {
     if (flag[i] != 1) continue;
-    int64_t nd = 0;
     for (int64_t j = rs[i] + 1; j < rs[i + 1]; ++j) {
       if (fabs(v[j]) < beta[i]) continue;
-      if (flag[cn[j]] == -1) dep[nd++] = cn[j];
+      if (flag[cn[j]] == -1) dep[cn[j]] = i;
     }
     int is_FF = 0;
     for (int64_t j = rs[i] + 1; j < rs[i + 1]; ++j) {
@@ -487,10 +514,7 @@ static int project(const orc_csr *M, double alpha, orc_csr *P, orc_csr *Pt, int3
       for (int64_t j1 = rs[k] + 1; j1 < rs[k + 1]; ++j1) {
         int64_t k1 = cn[j1];
         if (flag[k1] != -1) continue;
-        int found = 0;
-        for (int64_t q = 0; q < nd; ++q)
-          if (dep[q] == k1) { found = 1; break; }
-        if (found) { is_FF = 0; break; }
+        if (dep[k1] == i) { is_FF = 0; break; }
       }
       if (is_FF) break;
     }
@@ -562,22 +586,21 @@ static int project(const orc_csr *M, double alpha, orc_csr *P, orc_csr *Pt, int3
         matrix_add(Pt, i, core_at[l], fabs(v[j] / aii));
         matrix_add(P, core_at[l], i, fabs(v[j] / aii));
       } else {
+        /* dep = Pt row i, ascending: a binary search answers the reference's
+         * std::find(dep_begin, dep_end, c1) */
         double d = 0.0;
         for (int64_t i1 = Pt->rowptr[l]; i1 < Pt->rowptr[l + 1]; ++i1) {
           int64_t c1 = Pt->cols[i1];
-          for (const int64_t *q = dep_b; q != dep_e; ++q)
-            if (*q == c1) { d += matrix_el(M, l, core_point[c1]); break; }
+          if (sorted_has(dep_b, dep_e, c1)) d += matrix_el(M, l, core_point[c1]);
         }
         if (fabs(d * aii) < 1e-16) continue;
         for (int64_t i1 = Pt->rowptr[l]; i1 < Pt->rowptr[l + 1]; ++i1) {
           int64_t c1 = Pt->cols[i1];
-          for (const int64_t *q = dep_b; q != dep_e; ++q)
-            if (*q == c1) {
-              double w = fabs(matrix_el(M, i, l) * matrix_el(M, l, core_point[c1]) / (d * aii));
-              matrix_add(Pt, i, c1, w);
-              matrix_add(P, c1, i, w);
-              break;
-            }
+          if (sorted_has(dep_b, dep_e, c1)) {
+            double w = fabs(matrix_el(M, i, l) * matrix_el(M, l, core_point[c1]) / (d * aii));
+            matrix_add(Pt, i, c1, w);
+            matrix_add(P, c1, i, w);
+          }
         }
       }
     }
