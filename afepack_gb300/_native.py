@@ -111,6 +111,7 @@ SIGNATURES = {
     "afp_amg_download_projection": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p],
     "afp_amg_solve": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_int, C.POINTER(SolveInfo)],
     "afp_amg_precondition": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],
+    "afp_amg_time_kernel": [C.c_void_p, C.c_int, C.c_int, C.c_int, c_f64p, c_f64p],
     "afp_pcg_solve": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.POINTER(SolveInfo)],
     "afp_pcg_solve_multi": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
                             C.POINTER(SolveInfo)],

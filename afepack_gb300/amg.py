@@ -111,6 +111,13 @@ class AMGSolver:
         N.call("afp_amg_download_projection", self.handle, level, None, N.ptr(ci), N.ptr(va))
         return rp, ci, va
 
+    def time_kernel(self, kind: int, level: int = 0, reps: int = 20):
+        """(mean ms, algorithmic bytes) of one unit: 0 GS sweep, 1 residual,
+        2 V-cycle, 3 FP64 fine SpMV (CUDA events on the library stream)."""
+        ms, nb = C.c_double(), C.c_double()
+        N.call("afp_amg_time_kernel", self.handle, kind, level, reps, C.byref(ms), C.byref(nb))
+        return ms.value, nb.value
+
     # solving
     def solve(self, x, r, tol: float = 0.0, step: int = 20, mode: int = 0):
         """step+1 V-cycles from x, in place (AMGSolver::solve)."""

@@ -463,6 +463,105 @@ void check_finite(double v, const char* what) {
   if (!std::isfinite(v)) fail(AFP_ERR_BREAKDOWN, std::string("non-finite ") + what);
 }
 
+// ------------------------------------------------------------------------
+// CG as one CUDA graph: the first iteration, then a conditional WHILE node
+// whose body is a whole iteration (V-cycle included); a one-thread kernel at
+// the end of each iteration sets the loop condition from r.r, so the host
+// synchronises once per solve instead of once per iteration.
+// Device scalars: s[0] rz, s[1] p.q, s[2] r.r, s[3] rz', s[4] b.b,
+// s[6] tol^2 b.b; loopvars = [iterations done, limit].
+__global__ void k_pcg_check(const double* __restrict__ s, int* __restrict__ it, cudaGraphConditionalHandle handle) {
+  const int k = ++it[0];
+  const double rr = s[2];
+  const bool cont = (rr > s[6]) && (k < it[1]) && isfinite(rr);
+  cudaGraphSetConditional(handle, cont ? 1u : 0u);
+}
+
+__global__ void k_copy_scalar(double* s, int from, int to) { s[to] = s[from]; }
+
+// z = M r on the solver's level-0 buffers, launched into the current capture
+void precondition_inline(afp_amg* h) {
+  afp_context* ctx = h->ctx;
+  const int64_t n = h->lv[0].n;
+  if (h->opts.precision == AFP_PRECISION_MIXED) {
+    convert<double, float>(ctx, n, h->r.get(), h->r32.get());
+    vcycle<float, __nv_bfloat16>(h, h->z32.get(), h->r32.get(), true);
+    convert<float, double>(ctx, n, h->z32.get(), h->z.get());
+  } else {
+    vcycle<double, double>(h, h->z.get(), h->r.get(), true);
+  }
+}
+
+void pcg_iteration_tail(afp_amg* h, double* s, cudaGraphConditionalHandle handle) {
+  afp_context* ctx = h->ctx;
+  const Level& L0 = h->lv[0];
+  spmv_dot(ctx, L0.A<double>(), h->p.get(), h->q.get(), s + 1);
+  cg_update_xr(ctx, L0.n, s, 0, 1, h->x.get(), h->r.get(), h->p.get(), h->q.get(), s + 2);
+  k_pcg_check<<<1, 1, 0, ctx->stream>>>(s, h->loopvars.get(), handle);
+  check_launch(ctx, "cg check");
+}
+
+cudaGraphExec_t& loop_graph(afp_amg* h) {
+  afp_context* ctx = h->ctx;
+  const int pi = h->opts.precision == AFP_PRECISION_MIXED ? 1 : 0;
+  cudaGraphExec_t& exec = pi ? h->loop32 : h->loop64;
+  if (exec != nullptr) return exec;
+  const int64_t n = h->lv[0].n;
+  double* s = ctx->d_scalars;
+  if (h->loopvars.size() == 0) h->loopvars.alloc(ctx, 2);
+  cudaGraph_t g;
+  AFP_CUDA(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle handle;
+  AFP_CUDA(cudaGraphConditionalHandleCreate(&handle, g, 0, 0));
+  const int64_t n0 = ctx->launches.n;
+  AFP_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+  try {
+    precondition_inline(h);
+    dot(ctx, n, h->r.get(), h->z.get(), s + 0);
+    AFP_CUDA(cudaMemcpyAsync(h->p.get(), h->z.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    pcg_iteration_tail(h, s, handle);
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cg;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    AFP_CUDA(cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, nullptr, &nd));
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    AFP_CUDA(cudaGraphAddNode(&node, cg, deps, nullptr, nd, &cp));
+    AFP_CUDA(cudaStreamUpdateCaptureDependencies(ctx->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  } catch (...) {
+    cudaStreamEndCapture(ctx->stream, &g);
+    cudaGraphDestroy(g);
+    throw;
+  }
+  AFP_CUDA(cudaStreamEndCapture(ctx->stream, &g));
+  const int64_t n1 = ctx->launches.n;
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  AFP_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  try {
+    precondition_inline(h);
+    dot(ctx, n, h->r.get(), h->z.get(), s + 3);
+    cg_update_p(ctx, n, s, 3, 0, h->z.get(), h->p.get());
+    k_copy_scalar<<<1, 1, 0, ctx->stream>>>(s, 3, 0);
+    check_launch(ctx, "copy scalar");
+    pcg_iteration_tail(h, s, handle);
+  } catch (...) {
+    cudaStreamEndCapture(ctx->stream, &body);
+    cudaGraphDestroy(g);
+    throw;
+  }
+  AFP_CUDA(cudaStreamEndCapture(ctx->stream, &body));
+  AFP_CUDA(cudaGraphInstantiate(&exec, g, 0));
+  AFP_CUDA(cudaGraphDestroy(g));
+  h->loop_pre_nodes[pi] = n1 - n0;
+  h->loop_body_nodes[pi] = ctx->launches.n - n1;
+  ctx->launches.n = n0;
+  return exec;
+}
+
 void pcg(afp_amg* h, double* x_user, const double* b_user, double tol, int maxit, afp_solve_info* info) {
   afp_context* ctx = h->ctx;
   const Level& L0 = h->lv[0];
@@ -490,7 +589,25 @@ void pcg(afp_amg* h, double* x_user, const double* b_user, double tol, int maxit
   const double init = rel;
   int it = 0;
   bool conv = rel <= tol;
-  if (!conv) {
+  static const bool host_loop = std::getenv("AFP_HOST_LOOP") != nullptr;
+  if (!conv && maxit > 0 && !host_loop) {
+    const int pi = h->opts.precision == AFP_PRECISION_MIXED ? 1 : 0;
+    cudaGraphExec_t exec = loop_graph(h);
+    ctx->h_scalars[0] = tol * tol * hs[4];
+    copy(ctx, s + 6, ctx->h_scalars, sizeof(double));
+    int lv[2] = {0, maxit};
+    h->loopvars.upload(lv, 2);
+    AFP_CUDA(cudaGraphLaunch(exec, ctx->stream));
+    double rr;
+    copy(ctx, &rr, s + 2, sizeof(double));
+    h->loopvars.download(lv, 2);
+    sync(ctx);
+    it = lv[0];
+    ctx->launches.n += h->loop_pre_nodes[pi] + (int64_t)(it - 1) * h->loop_body_nodes[pi];
+    rel = std::sqrt(rr) / bn;
+    check_finite(rel, "residual");
+    conv = rel <= tol;
+  } else if (!conv) {
     precondition(h);  // z = M r
     dot(ctx, n, h->r.get(), h->z.get(), s + 0);
     AFP_CUDA(cudaMemcpyAsync(h->p.get(), h->z.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -676,6 +793,92 @@ afp_status afp_amg_solve(afp_amg* h, double* x, const double* r, double tol, int
       info->initial_residual = init;
       info->final_residual = fin;
       info->seconds = ms * 1e-3;
+    }
+  });
+}
+
+afp_status afp_amg_time_kernel(afp_amg* h, int kind, int level, int reps, double* ms, double* bytes) {
+  return guarded([&] {
+    AFP_REQUIRE(h && ms && bytes && reps > 0 && kind >= 0 && kind <= 3, AFP_ERR_INVALID, "bad argument");
+    AFP_REQUIRE(level >= 0 && level < std::max(1, h->t), AFP_ERR_INVALID, "level is not a smoothed level");
+    afp_context* ctx = h->ctx;
+    bind(ctx);
+    const bool mixed = h->opts.precision == AFP_PRECISION_MIXED;
+    const Level& L = h->lv[level];
+    const double v = mixed ? 4.0 : 8.0;
+    // inputs: r = 1, x = 0 on the level (level 0 uses the solver's vectors)
+    const int64_t n = L.n;
+    if (mixed) {
+      std::vector<float> one(n, 1.0f);
+      copy(ctx, level == 0 ? h->r32.get() : L.r32.get(), one.data(), sizeof(float) * n);
+      fill_zero<float>(ctx, n, level == 0 ? h->z32.get() : L.x32.get());
+    } else {
+      std::vector<double> one(n, 1.0);
+      copy(ctx, level == 0 ? h->r.get() : L.r.get(), one.data(), sizeof(double) * n);
+      fill_zero<double>(ctx, n, level == 0 ? h->z.get() : L.x.get());
+    }
+    auto unit = [&]() {
+      if (kind == 0 || kind == 1) {
+        if (mixed) {
+          float* x = level == 0 ? h->z32.get() : L.x32.get();
+          const float* r = level == 0 ? h->r32.get() : L.r32.get();
+          if (kind == 0) {
+            afp_amg_opts keep = h->opts;
+            h->opts.smooth_step = 1;
+            smooth<float>(h, level, x, r, false);
+            h->opts = keep;
+          } else {
+            residual<float>(ctx, L.A<float>(), x, r, L.tmp32.get());
+          }
+        } else {
+          double* x = level == 0 ? h->z.get() : L.x.get();
+          const double* r = level == 0 ? h->r.get() : L.r.get();
+          if (kind == 0) {
+            afp_amg_opts keep = h->opts;
+            h->opts.smooth_step = 1;
+            smooth<double>(h, level, x, r, false);
+            h->opts = keep;
+          } else {
+            residual<double>(ctx, L.A<double>(), x, r, L.tmp.get());
+          }
+        }
+      } else if (kind == 2) {
+        if (mixed) vcycle<float, __nv_bfloat16>(h, h->z32.get(), h->r32.get(), true);
+        else vcycle<double, double>(h, h->z.get(), h->r.get(), true);
+      } else {
+        spmv<double, double>(ctx, h->lv[0].A<double>(), h->p.get(), h->q.get(), false);
+      }
+    };
+    unit();  // warm
+    cudaEvent_t e0, e1;
+    AFP_CUDA(cudaEventCreate(&e0));
+    AFP_CUDA(cudaEventCreate(&e1));
+    AFP_CUDA(cudaEventRecord(e0, ctx->stream));
+    for (int i = 0; i < reps; ++i) unit();
+    AFP_CUDA(cudaEventRecord(e1, ctx->stream));
+    sync(ctx);
+    float t = 0;
+    AFP_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / reps;
+    const double mat = (double)L.nnz * (v + 4) + 4.0 * (n + 1);
+    if (kind == 0) *bytes = mat + 3.0 * n * v;           // read r, x gathers once, write x
+    else if (kind == 1) *bytes = mat + 3.0 * n * v;      // read x, r, write out
+    else if (kind == 3) *bytes = (double)h->lv[0].nnz * 12 + 4.0 * (h->lv[0].n + 1) + 2.0 * h->lv[0].n * 8;
+    else {
+      const double s = h->opts.smooth_step, vp = mixed ? 2.0 : 8.0;
+      double b = 0;
+      for (int l = 0; l < h->t; ++l) {
+        const Level& Q = h->lv[l];
+        const double m = (double)Q.nnz * (v + 4) + 4.0 * (Q.n + 1);
+        b += (2 * s + 1) * m + 2 * s * 3 * Q.n * v + 2 * Q.n * v;
+        b += 2.0 * Q.pnnz * (vp + 4) + 4.0 * (h->lv[l + 1].n + 1) + 4.0 * (Q.n + 1) + 3.0 * Q.n * v +
+             2.0 * h->lv[l + 1].n * v;
+      }
+      const double nt = (double)h->lv[h->t].n;
+      b += h->tail_dense ? nt * nt * v : 0.0;
+      *bytes = b;
     }
   });
 }

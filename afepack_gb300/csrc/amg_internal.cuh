@@ -80,10 +80,16 @@ struct afp_amg {
   cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
   int64_t graph64_nodes = 0, graph32_nodes = 0;
   std::unique_ptr<afp::MultiState> multi;
+  // whole-CG graphs (first iteration + conditional while loop), per precision
+  cudaGraphExec_t loop64 = nullptr, loop32 = nullptr;
+  int64_t loop_pre_nodes[2] = {0, 0}, loop_body_nodes[2] = {0, 0};
+  afp::DevBuf<int> loopvars;  // [iterations done, iteration limit]
 
   ~afp_amg() {
     if (graph64) cudaGraphExecDestroy(graph64);
     if (graph32) cudaGraphExecDestroy(graph32);
+    if (loop64) cudaGraphExecDestroy(loop64);
+    if (loop32) cudaGraphExecDestroy(loop32);
   }
 };
 

@@ -221,8 +221,7 @@ def run_ours(args):
             e2e_t.append(s0.elapsed_time(s1))
     e2e_t = np.array(e2e_t)
 
-    # ---- roofline of the V-cycle (mixed): bytes per V-cycle / time per V-cycle
-    vb = vcycle_bytes(amg32, 4, 2, 4)
+    # ---- roofline: kernels timed live with CUDA events on the library stream
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -230,13 +229,17 @@ def run_ours(args):
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     n0, nnz0, _ = levels[0]
-    it = results["mixed"]["pcg_iterations"]
-    # per iteration: one V-cycle + FP64 SpMV + ~10 vector passes
-    iter_bytes = vb + nnz0 * 12 + 4 * (n0 + 1) + 2 * n0 * 8 + 10 * n0 * 8
-    achieved = it * iter_bytes / (results["mixed"]["ms_mean"] * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": "PCG iteration (V-cycle + SpMV + vector ops), mixed",
-            "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
-            "traffic": None, "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"}
+    kernels = {}
+    for label, amg, kind in (("gs_sweep_level0_mixed", amg32, 0), ("residual_level0_mixed", amg32, 1),
+                             ("vcycle_mixed", amg32, 2), ("gs_sweep_level0_fp64", amg64, 0),
+                             ("vcycle_fp64", amg64, 2), ("spmv_fine_fp64", amg64, 3)):
+        ms, nbytes = amg.time_kernel(kind, 0, 20)
+        kernels[label] = {"ms": round(ms, 5), "bytes": int(nbytes), "GBps": round(nbytes / ms / 1e6, 1),
+                          "frac": round(nbytes / ms / 1e6 / hbm, 4)}
+    dom = kernels["gs_sweep_level0_mixed"]
+    roof = {"bound": "hbm", "kernel": "k_gs_class<float>: one Gauss-Seidel sweep (all colour classes) of level 0",
+            "achieved": dom["GBps"], "peak": hbm, "unit": "GB/s", "frac": dom["frac"], "traffic": None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s", "kernels": kernels}
 
     launches = ctx.launch_count()
     # CPU baseline (rank 0, N=1): the reference algorithm's solve on one core

@@ -182,6 +182,15 @@ afp_status afp_amg_download_level(const afp_amg *amg, int level, int32_t *rowptr
 afp_status afp_amg_download_projection(const afp_amg *amg, int level, int32_t *rowptr,
                                        int32_t *cols, double *vals);
 
+/* Measurement hook (no reference counterpart): runs `reps` times one unit of
+ * work on device-resident data and reports its mean device time (CUDA events
+ * on the context's stream) and its algorithmic bytes (compulsory traffic:
+ * each array once per pass).  kind: 0 = one Gauss-Seidel sweep over all
+ * colour classes of `level`, 1 = the residual SpMV of `level`, 2 = one
+ * V-cycle, 3 = the FP64 fine-level SpMV of the CG.  The precision is the
+ * solver's. */
+afp_status afp_amg_time_kernel(afp_amg *amg, int kind, int level, int reps, double *ms, double *bytes);
+
 /* AMGSolver::solve(x, r, tol, step, mode) (src/AMGSolver.cpp:549-639):
  * step+1 V-cycles starting from x; tol only decides `converged`
  * (l1 residual < tol * initial l1 residual; tol == 0 uses the solver's). */
