@@ -31,7 +31,7 @@ SOURCES = [
     ("coarsen_host.cpp", []),
     ("server.cpp", []),
 ]
-HEADERS = ["common.cuh", "kernels.cuh", "solve.cuh", "amg_internal.cuh", "quadrature_tables.h"]
+HEADERS = ["common.cuh", "kernels.cuh", "solve.cuh", "amg_internal.cuh", "launch.cuh", "quadrature_tables.h"]
 
 
 def _nvcc() -> str:

@@ -19,6 +19,7 @@
 #include <numeric>
 
 #include "amg_internal.cuh"
+#include "launch.cuh"
 
 using namespace afp;
 
@@ -471,13 +472,17 @@ void check_finite(double v, const char* what) {
 // Device scalars: s[0] rz, s[1] p.q, s[2] r.r, s[3] rz', s[4] b.b,
 // s[6] tol^2 b.b; loopvars = [iterations done, limit].
 __global__ void k_pcg_check(const double* __restrict__ s, int* __restrict__ it, cudaGraphConditionalHandle handle) {
+  pdl_wait();
   const int k = ++it[0];
   const double rr = s[2];
   const bool cont = (rr > s[6]) && (k < it[1]) && isfinite(rr);
   cudaGraphSetConditional(handle, cont ? 1u : 0u);
 }
 
-__global__ void k_copy_scalar(double* s, int from, int to) { s[to] = s[from]; }
+__global__ void k_copy_scalar(double* s, int from, int to) {
+  pdl_wait();
+  s[to] = s[from];
+}
 
 // z = M r on the solver's level-0 buffers, launched into the current capture
 void precondition_inline(afp_amg* h) {
@@ -497,7 +502,7 @@ void pcg_iteration_tail(afp_amg* h, double* s, cudaGraphConditionalHandle handle
   const Level& L0 = h->lv[0];
   spmv_dot(ctx, L0.A<double>(), h->p.get(), h->q.get(), s + 1);
   cg_update_xr(ctx, L0.n, s, 0, 1, h->x.get(), h->r.get(), h->p.get(), h->q.get(), s + 2);
-  k_pcg_check<<<1, 1, 0, ctx->stream>>>(s, h->loopvars.get(), handle);
+  launch_pdl(ctx->stream, 1, 1, 0, k_pcg_check, (const double*)s, h->loopvars.get(), handle);
   check_launch(ctx, "cg check");
 }
 
@@ -545,7 +550,7 @@ cudaGraphExec_t& loop_graph(afp_amg* h) {
     precondition_inline(h);
     dot(ctx, n, h->r.get(), h->z.get(), s + 3);
     cg_update_p(ctx, n, s, 3, 0, h->z.get(), h->p.get());
-    k_copy_scalar<<<1, 1, 0, ctx->stream>>>(s, 3, 0);
+    launch_pdl(ctx->stream, 1, 1, 0, k_copy_scalar, s, 3, 0);
     check_launch(ctx, "copy scalar");
     pcg_iteration_tail(h, s, handle);
   } catch (...) {

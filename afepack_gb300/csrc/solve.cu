@@ -10,6 +10,7 @@
 // Reductions are deterministic: each block writes a partial sum and the last
 // block to finish adds the partials in block order.
 #include "kernels.cuh"
+#include "launch.cuh"
 #include "solve.cuh"
 
 namespace afp {
@@ -62,6 +63,7 @@ __device__ __forceinline__ T group_sum(T s) {
 template <int VEC, class V, class X, bool ADD>
 __global__ void k_spmv(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci, const V* __restrict__ va,
                        const X* __restrict__ x, X* __restrict__ y) {
+  pdl_wait();
   using A = typename Acc<X>::type;
   const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
   const int lane = threadIdx.x % VEC;
@@ -75,6 +77,7 @@ __global__ void k_spmv(int64_t m, const int* __restrict__ rp, const int* __restr
 template <int VEC, class X>
 __global__ void k_residual(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci, const X* __restrict__ va,
                            const X* __restrict__ x, const X* __restrict__ r, X* __restrict__ out) {
+  pdl_wait();
   using A = typename Acc<X>::type;
   const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
   const int lane = threadIdx.x % VEC;
@@ -88,6 +91,7 @@ __global__ void k_residual(int64_t m, const int* __restrict__ rp, const int* __r
 template <int VEC, class X>
 __global__ void k_gs_class(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
                            const X* __restrict__ va, X* __restrict__ x, const X* __restrict__ r) {
+  pdl_wait();
   using A = typename Acc<X>::type;
   const int64_t row = r0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
   const int lane = threadIdx.x % VEC;
@@ -105,6 +109,7 @@ template <int VEC, class X>
 __global__ void k_jacobi_l1(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
                             const X* __restrict__ va, const X* __restrict__ x, const X* __restrict__ r,
                             const X* __restrict__ d, X* __restrict__ tmp) {
+  pdl_wait();
   using A = typename Acc<X>::type;
   const int64_t row = r0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
   const int lane = threadIdx.x % VEC;
@@ -117,12 +122,14 @@ __global__ void k_jacobi_l1(int64_t r0, int64_t r1, const int* __restrict__ rp, 
 
 template <class X>
 __global__ void k_copy_range(int64_t n, const X* __restrict__ src, X* __restrict__ dst) {
+  pdl_wait();
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = src[i];
 }
 
 template <class X>
 __global__ void k_dense_gemv(int64_t n, const X* __restrict__ M, const X* __restrict__ r, X* __restrict__ x) {
+  pdl_wait();
   using A = typename Acc<X>::type;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x & 31;
@@ -136,18 +143,21 @@ __global__ void k_dense_gemv(int64_t n, const X* __restrict__ M, const X* __rest
 template <class X>
 __global__ void k_diag_solve(int64_t n, const int* __restrict__ rp, const X* __restrict__ va, const X* __restrict__ r,
                              X* __restrict__ x) {
+  pdl_wait();
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) x[i] = r[i] / va[rp[i]];
 }
 
 template <class A, class B>
 __global__ void k_convert(int64_t n, const A* __restrict__ in, B* __restrict__ out) {
+  pdl_wait();
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = (B)in[i];
 }
 template <>
 __global__ void k_convert<double, __nv_bfloat16>(int64_t n, const double* __restrict__ in,
                                                  __nv_bfloat16* __restrict__ out) {
+  pdl_wait();
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = __double2bfloat16(in[i]);
 }
@@ -164,6 +174,7 @@ __global__ void k_scatter(int64_t n, const int* __restrict__ perm, const double*
 }
 
 __global__ void k_axpy(int64_t n, double alpha, const double* __restrict__ x, double* __restrict__ y) {
+  pdl_wait();
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) y[i] += alpha * x[i];
 }
@@ -176,6 +187,7 @@ __global__ void k_strided_copy(int64_t n, const double* __restrict__ src, int64_
 
 template <class X>
 __global__ void k_zero(int64_t n, X* __restrict__ x) {
+  pdl_wait();
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) x[i] = (X)0;
 }
@@ -224,6 +236,7 @@ __device__ __forceinline__ void finish_reduction(double partial, double* dst, Re
 
 __global__ void k_dot(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* dst,
                       RedScratch rs) {
+  pdl_wait();
   double s = 0;
   for (int64_t i = (int64_t)blockIdx.x * BLK + threadIdx.x; i < n; i += (int64_t)gridDim.x * BLK) s += a[i] * b[i];
   s = block_sum(s);
@@ -234,6 +247,7 @@ template <int VEC>
 __global__ void k_spmv_dot(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci,
                            const double* __restrict__ va, const double* __restrict__ p, double* __restrict__ y,
                            double* dst, RedScratch rs) {
+  pdl_wait();
   // warps stride over the rows uniformly so every lane joins each shuffle
   constexpr int GPW = 32 / VEC;
   const int lane = threadIdx.x % VEC, sub = (threadIdx.x & 31) / VEC;
@@ -257,6 +271,7 @@ __global__ void k_spmv_dot(int64_t m, const int* __restrict__ rp, const int* __r
 __global__ void k_cg_update_xr(int64_t n, const double* __restrict__ sc, int num, int den, double* __restrict__ x,
                                double* __restrict__ r, const double* __restrict__ p, const double* __restrict__ q,
                                double* dst, RedScratch rs) {
+  pdl_wait();
   const double alpha = sc[num] / sc[den];
   double s = 0;
   for (int64_t i = (int64_t)blockIdx.x * BLK + threadIdx.x; i < n; i += (int64_t)gridDim.x * BLK) {
@@ -271,6 +286,7 @@ __global__ void k_cg_update_xr(int64_t n, const double* __restrict__ sc, int num
 
 __global__ void k_cg_update_p(int64_t n, const double* __restrict__ sc, int num, int den, const double* __restrict__ z,
                               double* __restrict__ p) {
+  pdl_wait();
   const double beta = sc[num] / sc[den];
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = z[i] + beta * p[i];
@@ -401,8 +417,8 @@ void spmv(const afp_context* ctx, const CSRView<V>& A, const X* x, X* y, bool ad
   launch_vec(A.vec, [&](auto VEC) {
     constexpr int W = decltype(VEC)::value;
     unsigned grid = grid_for(A.m * W, BLK);
-    if (add) k_spmv<W, V, X, true><<<grid, BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.cols, A.vals, x, y);
-    else k_spmv<W, V, X, false><<<grid, BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.cols, A.vals, x, y);
+    if (add) launch_pdl(ctx->stream, grid, BLK, 0, k_spmv<W, V, X, true>, A.m, A.rowptr, A.cols, A.vals, x, y);
+    else launch_pdl(ctx->stream, grid, BLK, 0, k_spmv<W, V, X, false>, A.m, A.rowptr, A.cols, A.vals, x, y);
   });
   check_launch(ctx, "spmv");
 }
@@ -411,7 +427,8 @@ template <class X>
 void residual(const afp_context* ctx, const CSRView<X>& A, const X* x, const X* r, X* out) {
   launch_vec(A.vec, [&](auto VEC) {
     constexpr int W = decltype(VEC)::value;
-    k_residual<W, X><<<grid_for(A.m * W, BLK), BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.cols, A.vals, x, r, out);
+    launch_pdl(ctx->stream, grid_for(A.m * W, BLK), BLK, 0, k_residual<W, X>, A.m, A.rowptr, A.cols, A.vals, x, r,
+               out);
   });
   check_launch(ctx, "residual");
 }
@@ -421,7 +438,8 @@ void gs_class(const afp_context* ctx, const CSRView<X>& A, int64_t r0, int64_t r
   if (r1 <= r0) return;
   launch_vec(A.vec, [&](auto VEC) {
     constexpr int W = decltype(VEC)::value;
-    k_gs_class<W, X><<<grid_for((r1 - r0) * W, BLK), BLK, 0, ctx->stream>>>(r0, r1, A.rowptr, A.cols, A.vals, x, r);
+    launch_pdl(ctx->stream, grid_for((r1 - r0) * W, BLK), BLK, 0, k_gs_class<W, X>, r0, r1, A.rowptr, A.cols, A.vals,
+               x, r);
   });
   check_launch(ctx, "gauss-seidel class");
 }
@@ -432,29 +450,29 @@ void jacobi_l1_class(const afp_context* ctx, const CSRView<X>& A, int64_t r0, in
   if (r1 <= r0) return;
   launch_vec(A.vec, [&](auto VEC) {
     constexpr int W = decltype(VEC)::value;
-    k_jacobi_l1<W, X><<<grid_for((r1 - r0) * W, BLK), BLK, 0, ctx->stream>>>(r0, r1, A.rowptr, A.cols, A.vals, x, r,
-                                                                             l1diag, tmp);
+    launch_pdl(ctx->stream, grid_for((r1 - r0) * W, BLK), BLK, 0, k_jacobi_l1<W, X>, r0, r1, A.rowptr, A.cols,
+               A.vals, (const X*)x, r, l1diag, tmp);
   });
   check_launch(ctx, "l1-jacobi class");
-  k_copy_range<X><<<grid_for(r1 - r0, BLK), BLK, 0, ctx->stream>>>(r1 - r0, tmp, x + r0);
+  launch_pdl(ctx->stream, grid_for(r1 - r0, BLK), BLK, 0, k_copy_range<X>, r1 - r0, (const X*)tmp, x + r0);
   check_launch(ctx, "l1-jacobi copy");
 }
 
 template <class X>
 void dense_gemv(const afp_context* ctx, int64_t n, const X* Ainv, const X* r, X* x) {
-  k_dense_gemv<X><<<grid_for(n * 32, BLK), BLK, 0, ctx->stream>>>(n, Ainv, r, x);
+  launch_pdl(ctx->stream, grid_for(n * 32, BLK), BLK, 0, k_dense_gemv<X>, n, Ainv, r, x);
   check_launch(ctx, "dense gemv");
 }
 
 template <class X>
 void diag_solve(const afp_context* ctx, const CSRView<X>& A, const X* r, X* x) {
-  k_diag_solve<X><<<grid_for(A.m, BLK), BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.vals, r, x);
+  launch_pdl(ctx->stream, grid_for(A.m, BLK), BLK, 0, k_diag_solve<X>, A.m, A.rowptr, A.vals, r, x);
   check_launch(ctx, "diagonal solve");
 }
 
 template <class A, class B>
 void convert(const afp_context* ctx, int64_t n, const A* in, B* out) {
-  k_convert<A, B><<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, in, out);
+  launch_pdl(ctx->stream, grid_for(n, BLK), BLK, 0, k_convert<A, B>, n, in, out);
   check_launch(ctx, "convert");
 }
 
@@ -480,33 +498,33 @@ void strided_copy(const afp_context* ctx, int64_t n, const double* src, int64_t 
 
 template <class X>
 void fill_zero(const afp_context* ctx, int64_t n, X* x) {
-  k_zero<X><<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, x);
+  launch_pdl(ctx->stream, grid_for(n, BLK), BLK, 0, k_zero<X>, n, x);
   check_launch(ctx, "zero");
 }
 
 void dot(const afp_context* ctx, int64_t n, const double* a, const double* b, double* dst) {
-  k_dot<<<red_grid(ctx, n), BLK, 0, ctx->stream>>>(n, a, b, dst, RedScratch{ctx->d_partials, ctx->d_retire});
+  launch_pdl(ctx->stream, red_grid(ctx, n), BLK, 0, k_dot, n, a, b, dst, RedScratch{ctx->d_partials, ctx->d_retire});
   check_launch(ctx, "dot");
 }
 
 void spmv_dot(const afp_context* ctx, const CSRView<double>& A, const double* p, double* y, double* dst) {
   launch_vec(A.vec, [&](auto VEC) {
     constexpr int W = decltype(VEC)::value;
-    k_spmv_dot<W><<<red_grid(ctx, A.m * W), BLK, 0, ctx->stream>>>(A.m, A.rowptr, A.cols, A.vals, p, y, dst,
-                                                                   RedScratch{ctx->d_partials, ctx->d_retire});
+    launch_pdl(ctx->stream, red_grid(ctx, A.m * W), BLK, 0, k_spmv_dot<W>, A.m, A.rowptr, A.cols, A.vals, p, y, dst,
+               RedScratch{ctx->d_partials, ctx->d_retire});
   });
   check_launch(ctx, "spmv+dot");
 }
 
 void cg_update_xr(const afp_context* ctx, int64_t n, const double* s, int num, int den, double* x, double* r,
                   const double* p, const double* q, double* dst) {
-  k_cg_update_xr<<<red_grid(ctx, n), BLK, 0, ctx->stream>>>(n, s, num, den, x, r, p, q, dst,
-                                                            RedScratch{ctx->d_partials, ctx->d_retire});
+  launch_pdl(ctx->stream, red_grid(ctx, n), BLK, 0, k_cg_update_xr, n, s, num, den, x, r, p, q, dst,
+             RedScratch{ctx->d_partials, ctx->d_retire});
   check_launch(ctx, "cg update x r");
 }
 
 void cg_update_p(const afp_context* ctx, int64_t n, const double* s, int num, int den, const double* z, double* p) {
-  k_cg_update_p<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, s, num, den, z, p);
+  launch_pdl(ctx->stream, grid_for(n, BLK), BLK, 0, k_cg_update_p, n, s, num, den, z, p);
   check_launch(ctx, "cg update p");
 }
 
