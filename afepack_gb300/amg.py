@@ -30,7 +30,8 @@ def default_opts() -> N.AMGOpts:
 class AMGSolver:
     def __init__(self, M: SparseMatrix | None = None, tol: float = 1.0e-12, s: int = 3, nmpo: int = 50,
                  nmpsd: float = 0.382, alp: float = 0.25, *, precision: int = FP64, dense_tail: int | None = None,
-                 max_colors: int | None = None, symmetric: bool = True, coarse_colors: int | None = None):
+                 max_colors: int | None = None, symmetric: bool = True, coarse_colors: int | None = None,
+                 interp_bf16: bool | None = None):
         self.opts = default_opts()
         self.opts.tolerance = tol
         self.opts.smooth_step = s
@@ -45,6 +46,8 @@ class AMGSolver:
         self.opts.symmetric = int(symmetric)
         if coarse_colors is not None:
             self.opts.coarse_colors = coarse_colors
+        if interp_bf16 is not None:
+            self.opts.interp_bf16 = int(interp_bf16)
         self.handle = None
         self.matrix = None
         if M is not None:

@@ -127,9 +127,7 @@ void vcycle(afp_amg* h, X* x0, const X* r0, bool zero_init) {
     if (l > 0 || zero_init) fill_zero<X>(ctx, L.n, x);
     smooth<X>(h, l, x, r, false);
     residual<X>(ctx, L.A<X>(), x, r, lvt<X>(h, l));
-    CSRView<PV> P{h->lv[l + 1].n, L.prp.get(), L.pci.get(), nullptr, L.pvec};
-    if constexpr (std::is_same<PV, double>::value) P.vals = L.pva.get();
-    else P.vals = L.pva16.get();
+    CSRView<PV> P{h->lv[l + 1].n, L.prp.get(), L.pci.get(), p_vals<PV>(L), L.pvec};
     spmv<PV, X>(ctx, P, lvt<X>(h, l), lvr<X>(h, l + 1), false);
   }
   X* xt = t == 0 ? x0 : lvx<X>(h, t);
@@ -146,12 +144,16 @@ void vcycle(afp_amg* h, X* x0, const X* r0, bool zero_init) {
     Level& L = h->lv[l];
     X* x = l == 0 ? x0 : lvx<X>(h, l);
     const X* r = l == 0 ? r0 : lvr<X>(h, l);
-    CSRView<PV> T{L.n, L.trp.get(), L.tci.get(), nullptr, L.tvec};
-    if constexpr (std::is_same<PV, double>::value) T.vals = L.tva.get();
-    else T.vals = L.tva16.get();
+    CSRView<PV> T{L.n, L.trp.get(), L.tci.get(), pt_vals<PV>(L), L.tvec};
     spmv<PV, X>(ctx, T, lvx<X>(h, l + 1), x, true);
     smooth<X>(h, l, x, r, h->opts.symmetric != 0);
   }
+}
+
+// Mixed-precision V-cycle: FP32 levels, P / P^T in BF16 or FP32 (opts.interp_bf16).
+void vcycle_mixed(afp_amg* h, float* x0, const float* r0) {
+  if (h->opts.interp_bf16) vcycle<float, __nv_bfloat16>(h, x0, r0, true);
+  else vcycle<float, float>(h, x0, r0, true);
 }
 
 // Captures (once) and replays the preconditioner z = V(r) on the solver's
@@ -166,7 +168,7 @@ void precondition(afp_amg* h) {
     const int64_t before = ctx->launches.n;
     AFP_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     try {
-      if (mixed) vcycle<float, __nv_bfloat16>(h, h->z32.get(), h->r32.get(), true);
+      if (mixed) vcycle_mixed(h, h->z32.get(), h->r32.get());
       else vcycle<double, double>(h, h->z.get(), h->r.get(), true);
     } catch (...) {
       cudaStreamEndCapture(ctx->stream, &g);
@@ -319,11 +321,16 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
     L.pnnz = P.nnz();
     L.pvec = pick_vec((double)P.nnz() / (double)P.m);
     L.tvec = pick_vec((double)P.nnz() / (double)P.n);
-    if (mixed) {
+    if (mixed && h->opts.interp_bf16) {
       L.pva16.alloc(ctx, P.nnz());
       L.tva16.alloc(ctx, P.nnz());
       convert<double, __nv_bfloat16>(ctx, P.nnz(), L.pva.get(), L.pva16.get());
       convert<double, __nv_bfloat16>(ctx, P.nnz(), L.tva.get(), L.tva16.get());
+    } else if (mixed) {
+      L.pva32.alloc(ctx, P.nnz());
+      L.tva32.alloc(ctx, P.nnz());
+      convert<double, float>(ctx, P.nnz(), L.pva.get(), L.pva32.get());
+      convert<double, float>(ctx, P.nnz(), L.tva.get(), L.tva32.get());
     }
     sync(ctx);
   }
@@ -490,7 +497,7 @@ void precondition_inline(afp_amg* h) {
   const int64_t n = h->lv[0].n;
   if (h->opts.precision == AFP_PRECISION_MIXED) {
     convert<double, float>(ctx, n, h->r.get(), h->r32.get());
-    vcycle<float, __nv_bfloat16>(h, h->z32.get(), h->r32.get(), true);
+    vcycle_mixed(h, h->z32.get(), h->r32.get());
     convert<float, double>(ctx, n, h->z32.get(), h->z.get());
   } else {
     vcycle<double, double>(h, h->z.get(), h->r.get(), true);
@@ -670,6 +677,7 @@ void afp_amg_default_opts(afp_amg_opts* o) {
   o->max_colors = 32;
   o->symmetric = 1;
   o->coarse_colors = 8;
+  o->interp_bf16 = 0;
 }
 
 afp_status afp_amg_setup(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out) {
@@ -848,7 +856,7 @@ afp_status afp_amg_time_kernel(afp_amg* h, int kind, int level, int reps, double
           }
         }
       } else if (kind == 2) {
-        if (mixed) vcycle<float, __nv_bfloat16>(h, h->z32.get(), h->r32.get(), true);
+        if (mixed) vcycle_mixed(h, h->z32.get(), h->r32.get());
         else vcycle<double, double>(h, h->z.get(), h->r.get(), true);
       } else {
         spmv<double, double>(ctx, h->lv[0].A<double>(), h->p.get(), h->q.get(), false);

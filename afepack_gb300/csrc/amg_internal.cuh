@@ -23,6 +23,7 @@ struct Level {
   DevBuf<int> prp, pci, trp, tci;
   DevBuf<double> pva, tva;
   DevBuf<__nv_bfloat16> pva16, tva16;
+  DevBuf<float> pva32, tva32;
   int64_t pnnz = 0;
   int pvec = 8, tvec = 8;
   DevBuf<int> perm;  // solve order -> reference order
@@ -41,6 +42,24 @@ template <>
 inline CSRView<float> Level::A<float>() const {
   return {n, rp.get(), ci.get(), va32.get(), vec};
 }
+
+// values of P (restriction) and P^T (prolongation) in the V-cycle's storage type
+template <class PV>
+const PV* p_vals(const Level& L);
+template <class PV>
+const PV* pt_vals(const Level& L);
+template <>
+inline const double* p_vals<double>(const Level& L) { return L.pva.get(); }
+template <>
+inline const float* p_vals<float>(const Level& L) { return L.pva32.get(); }
+template <>
+inline const __nv_bfloat16* p_vals<__nv_bfloat16>(const Level& L) { return L.pva16.get(); }
+template <>
+inline const double* pt_vals<double>(const Level& L) { return L.tva.get(); }
+template <>
+inline const float* pt_vals<float>(const Level& L) { return L.tva32.get(); }
+template <>
+inline const __nv_bfloat16* pt_vals<__nv_bfloat16>(const Level& L) { return L.tva16.get(); }
 
 // Work space of the batched multi-right-hand-side solver for k columns.
 struct MultiState {

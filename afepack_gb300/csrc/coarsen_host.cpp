@@ -32,11 +32,6 @@ inline double entry(const HostCSR& M, int i, int j) {
   return (p != hi && *p == j) ? M.vals[p - M.cols.data()] : 0.0;
 }
 
-inline bool sorted_contains(const int* b, const int* e, int key) {
-  const int* p = std::lower_bound(b, e, key);
-  return p != e && *p == key;
-}
-
 }  // namespace
 
 void host_project(const HostCSR& M, double alpha, std::vector<int>& flag, HostCSR& P, HostCSR& Pt) {
@@ -146,41 +141,43 @@ void host_project(const HostCSR& M, double alpha, std::vector<int>& flag, HostCS
     for (int c = 0; c < n_core; ++c)
       for (int q = P.rowptr[c]; q < P.rowptr[c + 1]; ++q) Pt.cols[cur[P.cols[q]]++] = c;
   }
-  // weights, accumulated per fine point in the reference's order
-  Pt.vals.assign(Pt.cols.size(), 0.0);
-  auto add_pt = [&](int i, int c, double w) {
-    const int* b = Pt.cols.data() + Pt.rowptr[i];
-    const int* e = Pt.cols.data() + Pt.rowptr[i + 1];
-    const int* p = std::lower_bound(b, e, c);
-    if (p != e && *p == c) Pt.vals[p - Pt.cols.data()] += w;
-  };
+  // weights, accumulated per fine point in the reference's order.
+  // a_lc[q] = M(l, core_point[c]) for the Pt entry q = (l, c): it depends on
+  // the entry only, so it is looked up once instead of once per neighbour i.
+  // The dependency set of i (its Pt row) is a marker array: dep_at[c] is the
+  // position of (i, c) in Pt while dep_row[c] == i.
+  const int64_t nnz_p = (int64_t)Pt.cols.size();
+  Pt.vals.assign(nnz_p, 0.0);
+  std::vector<double> a_lc(nnz_p);
+  for (int l = 0; l < m; ++l)
+    for (int q = Pt.rowptr[l]; q < Pt.rowptr[l + 1]; ++q) a_lc[q] = entry(M, l, core_point[Pt.cols[q]]);
+  std::vector<int> dep_row(n_core, -1), dep_at(n_core, 0);
   for (int i = 0; i < m; ++i) {
+    for (int q = Pt.rowptr[i]; q < Pt.rowptr[i + 1]; ++q) {
+      dep_row[Pt.cols[q]] = i;
+      dep_at[Pt.cols[q]] = q;
+    }
     const int k = core_at[i];
     if (k >= 0) {
-      add_pt(i, k, 1.0);
+      Pt.vals[dep_at[k]] += 1.0;
       continue;
     }
     double aii = v[rs[i]];
     for (int j = rs[i] + 1; j < rs[i + 1]; ++j)
       if (std::fabs(v[j]) < beta[i]) aii += v[j];
-    const int* dep_b = Pt.cols.data() + Pt.rowptr[i];
-    const int* dep_e = Pt.cols.data() + Pt.rowptr[i + 1];
     for (int j = rs[i] + 1; j < rs[i + 1]; ++j) {
       const int l = cn[j];
       if (std::fabs(v[j]) < beta[i]) continue;
       if (core_at[l] >= 0) {
-        add_pt(i, core_at[l], std::fabs(v[j] / aii));
+        if (dep_row[core_at[l]] == i) Pt.vals[dep_at[core_at[l]]] += std::fabs(v[j] / aii);
       } else {
         double d = 0.0;
-        for (int i1 = Pt.rowptr[l]; i1 < Pt.rowptr[l + 1]; ++i1) {
-          const int c1 = Pt.cols[i1];
-          if (sorted_contains(dep_b, dep_e, c1)) d += entry(M, l, core_point[c1]);
-        }
+        for (int i1 = Pt.rowptr[l]; i1 < Pt.rowptr[l + 1]; ++i1)
+          if (dep_row[Pt.cols[i1]] == i) d += a_lc[i1];
         if (std::fabs(d * aii) < 1e-16) continue;
         for (int i1 = Pt.rowptr[l]; i1 < Pt.rowptr[l + 1]; ++i1) {
           const int c1 = Pt.cols[i1];
-          if (sorted_contains(dep_b, dep_e, c1))
-            add_pt(i, c1, std::fabs(entry(M, i, l) * entry(M, l, core_point[c1]) / (d * aii)));
+          if (dep_row[c1] == i) Pt.vals[dep_at[c1]] += std::fabs(v[j] * a_lc[i1] / (d * aii));
         }
       }
     }

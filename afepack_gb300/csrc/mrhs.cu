@@ -424,9 +424,7 @@ void vcycle_m(afp_amg* h, MultiState& S) {
       k_residual_m<KPL, X><<<rows_grid(ctx, L.n), BLK, 0, ctx->stream>>>(L.n, A.rowptr, A.cols, A.vals, x, r,
                                                                         blk<X>(S, 2, l), k);
       check_launch(ctx, "mrhs residual");
-      const PV* pv;
-      if constexpr (std::is_same<PV, double>::value) pv = L.pva.get();
-      else pv = L.pva16.get();
+      const PV* pv = p_vals<PV>(L);
       const int64_t nc = h->lv[l + 1].n;
       k_spmm<KPL, PV, X, false><<<rows_grid(ctx, nc), BLK, 0, ctx->stream>>>(nc, L.prp.get(), L.pci.get(), pv,
                                                                             blk<X>(S, 2, l), blk<X>(S, 1, l + 1), k);
@@ -447,9 +445,7 @@ void vcycle_m(afp_amg* h, MultiState& S) {
     }
     for (int l = t - 1; l >= 0; --l) {
       Level& L = h->lv[l];
-      const PV* tv;
-      if constexpr (std::is_same<PV, double>::value) tv = L.tva.get();
-      else tv = L.tva16.get();
+      const PV* tv = pt_vals<PV>(L);
       k_spmm<KPL, PV, X, true><<<rows_grid(ctx, L.n), BLK, 0, ctx->stream>>>(L.n, L.trp.get(), L.tci.get(), tv,
                                                                             blk<X>(S, 0, l + 1), blk<X>(S, 0, l), k);
       check_launch(ctx, "mrhs prolongation");
@@ -514,7 +510,8 @@ void precondition_m(afp_amg* h) {
       if (S.mixed) {
         k_conv<double, float><<<grid_for(n0k, BLK), BLK, 0, ctx->stream>>>(n0k, S.Rs.get(), S.R32[0].get());
         check_launch(ctx, "mrhs to fp32");
-        vcycle_m<float, __nv_bfloat16>(h, S);
+        if (h->opts.interp_bf16) vcycle_m<float, __nv_bfloat16>(h, S);
+        else vcycle_m<float, float>(h, S);
         k_conv<float, double><<<grid_for(n0k, BLK), BLK, 0, ctx->stream>>>(n0k, S.X32[0].get(), S.Z.get());
         check_launch(ctx, "mrhs to fp64");
       } else {

@@ -141,6 +141,9 @@ typedef struct afp_amg_opts {
   int coarse_colors;    /* colour-class cap on levels >= 1 (default 8; 0 = use
                            max_colors); their long rows would otherwise need
                            dozens of sequential classes                         */
+  int interp_bf16;      /* mixed precision only: keep P and P^T in BF16 (1) or
+                           in FP32 (0, default: BF16 interpolation weights cost
+                           the 3D P1 solve about 1.5x the PCG iterations)       */
 } afp_amg_opts;
 
 typedef struct afp_solve_info {

@@ -243,15 +243,6 @@ static int64_t row_find(const orc_csr *a, int64_t i, int64_t j) {
   return (lo < e && a->cols[lo] == j) ? lo : -1;
 }
 
-static int sorted_has(const int64_t *b, const int64_t *e, int64_t key) {
-  const int64_t *lo = b, *hi = e;
-  while (lo < hi) {
-    const int64_t *mid = lo + (hi - lo) / 2;
-    if (*mid < key) lo = mid + 1; else hi = mid;
-  }
-  return lo < e && *lo == key;
-}
-
 /* SparseMatrix::add: adds v to entry (i, j) when it is in the pattern */
 static void matrix_add(orc_csr *a, int64_t i, int64_t j, double v) {
   int64_t k = row_find(a, i, j);
@@ -373,10 +364,44 @@ void orc_apply_dirichlet(orc_csr *a, double *f, const int32_t *dirichlet, const 
  * reference's (j, k, l) order, so running rows on several threads (OpenMP)
  * changes nothing in the result. */
 static int rap_with_pt(const orc_csr *P, const orc_csr *M, const orc_csr *Pt, orc_csr *A) {
-  const int64_t nc = P->m;
+  const int64_t nc = P->m, nf = M->m;
   A->m = A->n = nc;
   A->rowptr = (int64_t *)calloc(nc + 1, sizeof(int64_t));
-  /* pass 1: row lengths */
+  /* pass 1: row lengths.  Only the column SET of a row is needed here, so it
+   * is formed from the pattern of B = M Pt (row a of B = the union of the Pt
+   * rows of a's neighbours), built once: row i of the product is the union of
+   * the B rows of P row i's columns. */
+  int64_t *brp = (int64_t *)calloc(nf + 1, sizeof(int64_t));
+  int64_t *bci = NULL;
+  for (int pass = 0; pass < 2; ++pass) {
+#pragma omp parallel
+    {
+      char *flag = (char *)calloc(nc ? nc : 1, 1);
+      int64_t *index = (int64_t *)malloc(sizeof(int64_t) * (nc ? nc : 1));
+#pragma omp for schedule(dynamic, 256)
+      for (int64_t a = 0; a < nf; ++a) {
+        int64_t len = 0;
+        for (int64_t k = M->rowptr[a]; k < M->rowptr[a + 1]; ++k) {
+          int64_t b = M->cols[k];
+          for (int64_t l = Pt->rowptr[b]; l < Pt->rowptr[b + 1]; ++l) {
+            int64_t c = Pt->cols[l];
+            if (!flag[c]) { index[len++] = c; flag[c] = 1; }
+          }
+        }
+        for (int64_t q = 0; q < len; ++q) {
+          flag[index[q]] = 0;
+          if (pass == 1) bci[brp[a] + q] = index[q];
+        }
+        if (pass == 0) brp[a + 1] = len;
+      }
+      free(flag);
+      free(index);
+    }
+    if (pass == 0) {
+      for (int64_t a = 0; a < nf; ++a) brp[a + 1] += brp[a];
+      bci = (int64_t *)malloc(sizeof(int64_t) * (brp[nf] ? brp[nf] : 1));
+    }
+  }
 #pragma omp parallel
   {
     char *flag = (char *)calloc(nc ? nc : 1, 1);
@@ -388,12 +413,9 @@ static int rap_with_pt(const orc_csr *P, const orc_csr *M, const orc_csr *Pt, or
       index[0] = i;
       for (int64_t j = P->rowptr[i]; j < P->rowptr[i + 1]; ++j) {
         int64_t a = P->cols[j];
-        for (int64_t k = M->rowptr[a]; k < M->rowptr[a + 1]; ++k) {
-          int64_t b = M->cols[k];
-          for (int64_t l = Pt->rowptr[b]; l < Pt->rowptr[b + 1]; ++l) {
-            int64_t c = Pt->cols[l];
-            if (!flag[c]) { index[len++] = c; flag[c] = 1; }
-          }
+        for (int64_t q = brp[a]; q < brp[a + 1]; ++q) {
+          int64_t c = bci[q];
+          if (!flag[c]) { index[len++] = c; flag[c] = 1; }
         }
       }
       for (int64_t q = 0; q < len; ++q) flag[index[q]] = 0;
@@ -402,6 +424,8 @@ static int rap_with_pt(const orc_csr *P, const orc_csr *M, const orc_csr *Pt, or
     free(flag);
     free(index);
   }
+  free(brp);
+  free(bci);
   for (int64_t i = 0; i < nc; ++i) A->rowptr[i + 1] += A->rowptr[i];
   const int64_t nnz = A->rowptr[nc];
   A->cols = (int64_t *)malloc(sizeof(int64_t) * (nnz ? nnz : 1));
@@ -568,7 +592,18 @@ static int project(const orc_csr *M, double alpha, orc_csr *P, orc_csr *Pt, int3
   pattern_compress(n_core, square, ps, pslots, P);
   pattern_compress(m, square, ts, tslots, Pt);
   free(pslots); free(tslots); free(ps); free(ts);
+  /* a_lc[q] = M(l, core_point[c]) for the Pt entry q = (l, c), looked up once
+   * (it does not depend on the fine point i being interpolated); dep_row[c]
+   * == i marks the Pt row of i, the reference's "dep" list of i, whose
+   * std::find membership it answers. */
+  const int64_t nnz_t = Pt->rowptr[m];
+  double *a_lc = (double *)malloc(sizeof(double) * (nnz_t ? nnz_t : 1));
+  int64_t *dep_row = (int64_t *)malloc(sizeof(int64_t) * (n_core ? n_core : 1));
+  for (int64_t l = 0; l < m; ++l)
+    for (int64_t q = Pt->rowptr[l]; q < Pt->rowptr[l + 1]; ++q) a_lc[q] = matrix_el(M, l, core_point[Pt->cols[q]]);
+  for (int64_t c = 0; c < n_core; ++c) dep_row[c] = -1;
   for (int64_t i = 0; i < m; ++i) {
+    for (int64_t q = Pt->rowptr[i]; q < Pt->rowptr[i + 1]; ++q) dep_row[Pt->cols[q]] = i;
     int64_t k = core_at[i];
     if (k >= 0) {
       matrix_add(Pt, i, k, 1.0);
@@ -578,7 +613,6 @@ static int project(const orc_csr *M, double alpha, orc_csr *P, orc_csr *Pt, int3
     double aii = v[rs[i]];
     for (int64_t j = rs[i] + 1; j < rs[i + 1]; ++j)
       if (fabs(v[j]) < beta[i]) aii += v[j];
-    const int64_t *dep_b = Pt->cols + Pt->rowptr[i], *dep_e = Pt->cols + Pt->rowptr[i + 1];
     for (int64_t j = rs[i] + 1; j < rs[i + 1]; ++j) {
       int64_t l = cn[j];
       if (fabs(v[j]) < beta[i]) continue;
@@ -586,18 +620,15 @@ static int project(const orc_csr *M, double alpha, orc_csr *P, orc_csr *Pt, int3
         matrix_add(Pt, i, core_at[l], fabs(v[j] / aii));
         matrix_add(P, core_at[l], i, fabs(v[j] / aii));
       } else {
-        /* dep = Pt row i, ascending: a binary search answers the reference's
-         * std::find(dep_begin, dep_end, c1) */
         double d = 0.0;
-        for (int64_t i1 = Pt->rowptr[l]; i1 < Pt->rowptr[l + 1]; ++i1) {
-          int64_t c1 = Pt->cols[i1];
-          if (sorted_has(dep_b, dep_e, c1)) d += matrix_el(M, l, core_point[c1]);
-        }
+        for (int64_t i1 = Pt->rowptr[l]; i1 < Pt->rowptr[l + 1]; ++i1)
+          if (dep_row[Pt->cols[i1]] == i) d += a_lc[i1];
         if (fabs(d * aii) < 1e-16) continue;
         for (int64_t i1 = Pt->rowptr[l]; i1 < Pt->rowptr[l + 1]; ++i1) {
           int64_t c1 = Pt->cols[i1];
-          if (sorted_has(dep_b, dep_e, c1)) {
-            double w = fabs(matrix_el(M, i, l) * matrix_el(M, l, core_point[c1]) / (d * aii));
+          if (dep_row[c1] == i) {
+            /* v[j] is M(i, l): rows hold each column once */
+            double w = fabs(v[j] * a_lc[i1] / (d * aii));
             matrix_add(Pt, i, c1, w);
             matrix_add(P, c1, i, w);
           }
@@ -605,6 +636,7 @@ static int project(const orc_csr *M, double alpha, orc_csr *P, orc_csr *Pt, int3
       }
     }
   }
+  free(a_lc); free(dep_row);
   free(flag); free(beta); free(dep); free(core_point); free(core_at); free(row_length); free(col_length);
   return 0;
 }

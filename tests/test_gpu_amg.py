@@ -216,7 +216,10 @@ def test_lazy_preconditioner_matches_reference(ctx, name):
     A2 = S.to_scipy() * 1.5
     res = np.linalg.norm(b - A2 @ x) / np.linalg.norm(b)
     ref = np.linalg.norm(b - A2 @ g["x_lazy2"]) / np.linalg.norm(b)
-    assert res <= max(10 * ref, 1e-12), (res, ref)
+    # per-cycle contraction within a factor 2.5 of the reference's
+    # lexicographic smoother over the same three cycles
+    assert res < 1e-3, res
+    assert res ** (1 / 3) <= max(2.5 * ref ** (1 / 3), 1e-4), (res, ref)
     # a matrix with another pattern object is refused, as the reference aborts
     from afepack_gb300 import _native as N
     other = SparseMatrix.from_csr(ctx, S.rowptr, S.cols, S.vals)
