@@ -133,10 +133,8 @@ void vcycle(afp_amg* h, X* x0, const X* r0, bool zero_init) {
   X* xt = t == 0 ? x0 : lvx<X>(h, t);
   const X* rt = t == 0 ? r0 : lvr<X>(h, t);
   if (h->tail_dense) {
-    const X* inv;
-    if constexpr (std::is_same<X, double>::value) inv = h->tail_inv.get();
-    else inv = h->tail_inv32.get();
-    dense_gemv<X>(ctx, h->lv[t].n, inv, rt, xt);
+    if constexpr (std::is_same<X, double>::value) dense_gemv<double>(ctx, h->lv[t].n, h->tail_inv.get(), rt, xt);
+    else dense_gemv_df(ctx, h->lv[t].n, h->tail_hi.get(), h->tail_lo.get(), rt, xt);
   } else {
     diag_solve<X>(ctx, h->lv[t].A<X>(), rt, xt);
   }
@@ -341,8 +339,13 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
     if (!dense_inverse(ctx, T.A<double>(), h->tail_inv.get()))
       fail(AFP_ERR_SINGULAR, "coarsest matrix is singular");
     if (mixed) {
-      h->tail_inv32.alloc(ctx, T.n * T.n);
-      convert<double, float>(ctx, T.n * T.n, h->tail_inv.get(), h->tail_inv32.get());
+      // FP32 pair with FP64-class accuracy: a plain FP32 inverse summed in
+      // FP32 loses the coarse correction on ill-conditioned 3D tails
+      h->tail_hi.alloc(ctx, T.n * T.n);
+      h->tail_lo.alloc(ctx, T.n * T.n);
+      split_df(ctx, T.n * T.n, h->tail_inv.get(), h->tail_hi.get(), h->tail_lo.get());
+      sync(ctx);
+      h->tail_inv = DevBuf<double>();  // the FP64 V-cycle is not used at this precision
     }
   }
   if (mixed && !h->tail_dense) {

@@ -91,8 +91,8 @@ struct afp_amg {
   bool lazy = false;                      // hierarchy from lazyProject (AMGPreconditioner)
   std::vector<afp::HostCSR> refPt;        // lazyProject's own P^T, used by the Galerkin product
   std::shared_ptr<afp::Pattern> pat0;     // the fine matrix's pattern object (lazy re-setup check)
-  afp::DevBuf<double> tail_inv;
-  afp::DevBuf<float> tail_inv32;
+  afp::DevBuf<double> tail_inv;           // FP64 dense inverse (FP64 precision)
+  afp::DevBuf<float> tail_hi, tail_lo;    // the same as an FP32 pair hi + lo (mixed precision)
   // solver vectors (level-0 solve order)
   afp::DevBuf<double> b, x, r, z, p, q, tmp;
   afp::DevBuf<float> r32, z32;

@@ -13,6 +13,7 @@
 #include <cmath>
 
 #include "amg_internal.cuh"
+#include "df32.cuh"
 
 namespace afp {
 namespace {
@@ -181,6 +182,32 @@ __global__ void k_dense_gemm(int64_t n, const X* __restrict__ M, const X* __rest
     for (int q = 0; q < KPL; ++q) {
       const int c = lane + 32 * q;
       if (c < k) x[row * k + c] = (X)acc[q];
+    }
+  }
+}
+
+// FP32 V-cycle tail: X = (hi + lo) R with a double-float pair per column
+// (the single-column kernel's accumulation, see df32.cuh)
+template <int KPL>
+__global__ void k_dense_gemm_df(int64_t n, const float* __restrict__ hi, const float* __restrict__ lo,
+                                const float* __restrict__ r, float* __restrict__ x, int k) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t row = warp_id(); row < n; row += n_warps()) {
+    float sh[KPL], sl[KPL];
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) sh[q] = sl[q] = 0.f;
+    for (int64_t j = 0; j < n; ++j) {
+      const float a = hi[row * n + j], b = lo[row * n + j];
+#pragma unroll
+      for (int q = 0; q < KPL; ++q) {
+        const int c = lane + 32 * q;
+        if (c < k) df_add_prod(sh[q], sl[q], a, b, r[j * k + c]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) {
+      const int c = lane + 32 * q;
+      if (c < k) x[row * k + c] = __fadd_rn(sh[q], sl[q]);
     }
   }
 }
@@ -432,10 +459,12 @@ void vcycle_m(afp_amg* h, MultiState& S) {
     }
     const Level& T = h->lv[t];
     if (h->tail_dense) {
-      const X* inv;
-      if constexpr (std::is_same<X, double>::value) inv = h->tail_inv.get();
-      else inv = h->tail_inv32.get();
-      k_dense_gemm<KPL, X><<<rows_grid(ctx, T.n), BLK, 0, ctx->stream>>>(T.n, inv, blk<X>(S, 1, t), blk<X>(S, 0, t), k);
+      if constexpr (std::is_same<X, double>::value)
+        k_dense_gemm<KPL, X><<<rows_grid(ctx, T.n), BLK, 0, ctx->stream>>>(T.n, h->tail_inv.get(), blk<X>(S, 1, t),
+                                                                          blk<X>(S, 0, t), k);
+      else
+        k_dense_gemm_df<KPL><<<rows_grid(ctx, T.n), BLK, 0, ctx->stream>>>(T.n, h->tail_hi.get(), h->tail_lo.get(),
+                                                                          blk<X>(S, 1, t), blk<X>(S, 0, t), k);
       check_launch(ctx, "mrhs dense tail");
     } else {
       CSRView<X> A = T.A<X>();

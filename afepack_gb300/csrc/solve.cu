@@ -9,17 +9,27 @@
 //
 // Reductions are deterministic: each block writes a partial sum and the last
 // block to finish adds the partials in block order.
+#include <cstdlib>
+
+#include "df32.cuh"
 #include "kernels.cuh"
 #include "launch.cuh"
 #include "solve.cuh"
 
 namespace afp {
 
+// Lanes per row: the smallest power of two in [4, 32] with at most
+// `entries per lane` (default 1; AFP_ENTRIES_PER_LANE overrides it for
+// tuning) of the level's mean row length on each lane.
 int pick_vec(double avg) {
-  if (avg <= 4.5) return 4;
-  if (avg <= 10.0) return 8;
-  if (avg <= 20.0) return 16;
-  return 32;
+  static const double epl = [] {
+    const char* e = std::getenv("AFP_ENTRIES_PER_LANE");
+    const double v = e ? std::atof(e) : 0.0;
+    return v > 0.0 ? v : 1.0;
+  }();
+  int vec = 4;
+  while (vec < 32 && vec * epl < avg) vec *= 2;
+  return vec;
 }
 
 namespace {
@@ -60,16 +70,56 @@ __device__ __forceinline__ T group_sum(T s) {
   return s;
 }
 
+// Row loads ahead of griddepcontrol.wait.  The matrices of a solve are not
+// written by any kernel of the V-cycle / CG chain, so each thread loads its
+// row bounds and its first PF (column, value) pairs before waiting for the
+// predecessor grid; only the gathers of x (and reads of r) wait.  Under PDL
+// this overlaps two of the three dependent memory round trips of a row with
+// the predecessor's drain.  The products are summed in the same order as a
+// plain k = begin + lane, begin + lane + VEC, ... loop.
+template <int VEC>
+constexpr int prefetch_depth() {
+  return VEC >= 32 ? 8 : 4;
+}
+
+template <int VEC, class V>
+struct RowAhead {
+  static constexpr int PF = prefetch_depth<VEC>();
+  int k, e;  // first entry of this lane, row end
+  int c[PF];
+  V v[PF];
+  __device__ __forceinline__ void load(const int* __restrict__ ci, const V* __restrict__ va, int k0, int e0) {
+    k = k0;
+    e = e0;
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+      const int kk = k + q * VEC;
+      c[q] = kk < e ? ci[kk] : 0;
+      v[q] = kk < e ? va[kk] : V(0);
+    }
+  }
+  template <class A, class X>
+  __device__ __forceinline__ A dot(const int* __restrict__ ci, const V* __restrict__ va,
+                                   const X* __restrict__ x) const {
+    A s = 0;
+#pragma unroll
+    for (int q = 0; q < PF; ++q)
+      if (k + q * VEC < e) s += val_as<A>(v[q]) * (A)x[c[q]];
+    for (int kk = k + PF * VEC; kk < e; kk += VEC) s += val_as<A>(va[kk]) * (A)x[ci[kk]];
+    return s;
+  }
+};
+
 template <int VEC, class V, class X, bool ADD>
 __global__ void k_spmv(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci, const V* __restrict__ va,
                        const X* __restrict__ x, X* __restrict__ y) {
-  pdl_wait();
   using A = typename Acc<X>::type;
   const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
   const int lane = threadIdx.x % VEC;
-  A s = 0;
-  if (g < m)
-    for (int k = rp[g] + lane; k < rp[g + 1]; k += VEC) s += val_as<A>(va[k]) * (A)x[ci[k]];
+  RowAhead<VEC, V> row;
+  row.load(ci, va, g < m ? rp[g] + lane : 0, g < m ? rp[g + 1] : 0);
+  pdl_wait();
+  A s = row.template dot<A>(ci, va, x);
   s = group_sum<VEC>(s);
   if (g < m && lane == 0) y[g] = ADD ? (X)((A)y[g] + s) : (X)s;
 }
@@ -77,13 +127,13 @@ __global__ void k_spmv(int64_t m, const int* __restrict__ rp, const int* __restr
 template <int VEC, class X>
 __global__ void k_residual(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci, const X* __restrict__ va,
                            const X* __restrict__ x, const X* __restrict__ r, X* __restrict__ out) {
-  pdl_wait();
   using A = typename Acc<X>::type;
   const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
   const int lane = threadIdx.x % VEC;
-  A s = 0;
-  if (g < m)
-    for (int k = rp[g] + lane; k < rp[g + 1]; k += VEC) s += (A)va[k] * (A)x[ci[k]];
+  RowAhead<VEC, X> row;
+  row.load(ci, va, g < m ? rp[g] + lane : 0, g < m ? rp[g + 1] : 0);
+  pdl_wait();
+  A s = row.template dot<A>(ci, va, x);
   s = group_sum<VEC>(s);
   if (g < m && lane == 0) out[g] = (X)((A)r[g] - s);
 }
@@ -91,33 +141,34 @@ __global__ void k_residual(int64_t m, const int* __restrict__ rp, const int* __r
 template <int VEC, class X>
 __global__ void k_gs_class(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
                            const X* __restrict__ va, X* __restrict__ x, const X* __restrict__ r) {
-  pdl_wait();
   using A = typename Acc<X>::type;
   const int64_t row = r0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
   const int lane = threadIdx.x % VEC;
-  A s = 0;
-  int d = 0;
-  if (row < r1) {
-    d = rp[row];
-    for (int k = d + 1 + lane; k < rp[row + 1]; k += VEC) s += (A)va[k] * (A)x[ci[k]];
-  }
+  const bool on = row < r1;
+  const int d = on ? rp[row] : 0;
+  const X diag = on ? va[d] : X(1);
+  RowAhead<VEC, X> ahead;
+  ahead.load(ci, va, d + 1 + lane, on ? rp[row + 1] : 0);
+  pdl_wait();
+  A s = ahead.template dot<A>(ci, va, (const X*)x);
   s = group_sum<VEC>(s);
-  if (row < r1 && lane == 0) x[row] = (X)(((A)r[row] - s) / (A)va[d]);
+  if (on && lane == 0) x[row] = (X)(((A)r[row] - s) / (A)diag);
 }
 
 template <int VEC, class X>
 __global__ void k_jacobi_l1(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
                             const X* __restrict__ va, const X* __restrict__ x, const X* __restrict__ r,
                             const X* __restrict__ d, X* __restrict__ tmp) {
-  pdl_wait();
   using A = typename Acc<X>::type;
   const int64_t row = r0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / VEC;
   const int lane = threadIdx.x % VEC;
-  A s = 0;
-  if (row < r1)
-    for (int k = rp[row] + lane; k < rp[row + 1]; k += VEC) s += (A)va[k] * (A)x[ci[k]];
+  const bool on = row < r1;
+  RowAhead<VEC, X> ahead;
+  ahead.load(ci, va, on ? rp[row] + lane : 0, on ? rp[row + 1] : 0);
+  pdl_wait();
+  A s = ahead.template dot<A>(ci, va, x);
   s = group_sum<VEC>(s);
-  if (row < r1 && lane == 0) tmp[row - r0] = (X)((A)x[row] + ((A)r[row] - s) / (A)d[row - r0]);
+  if (on && lane == 0) tmp[row - r0] = (X)((A)x[row] + ((A)r[row] - s) / (A)d[row - r0]);
 }
 
 template <class X>
@@ -138,6 +189,48 @@ __global__ void k_dense_gemv(int64_t n, const X* __restrict__ M, const X* __rest
     for (int64_t j = lane; j < n; j += 32) s += (A)M[row * n + j] * (A)r[j];
   s = group_sum<32>(s);
   if (row < n && lane == 0) x[row] = (X)s;
+}
+
+__global__ void k_split_df(int64_t n, const double* __restrict__ in, float* __restrict__ hi,
+                           float* __restrict__ lo) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double d = in[i];
+  const float h = __double2float_rn(d);
+  hi[i] = h;
+  lo[i] = __double2float_rn(d - (double)h);
+}
+
+// One warp per row; each lane walks the row with stride 32 (coalesced loads of
+// hi and lo), accumulating a double-float pair; the pairs are merged across
+// the warp with TwoSum.
+__global__ void k_dense_gemv_df(int64_t n, const float* __restrict__ hi, const float* __restrict__ lo,
+                                const float* __restrict__ r, float* __restrict__ x) {
+  pdl_wait();
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;  // whole warps leave together
+  const float* h = hi + row * n;
+  const float* l = lo + row * n;
+  float sh = 0.f, sl = 0.f;
+  int64_t j = lane;
+  for (; j + 96 < n; j += 128) {
+    const float h0 = h[j], h1 = h[j + 32], h2 = h[j + 64], h3 = h[j + 96];
+    const float l0 = l[j], l1 = l[j + 32], l2 = l[j + 64], l3 = l[j + 96];
+    const float v0 = r[j], v1 = r[j + 32], v2 = r[j + 64], v3 = r[j + 96];
+    df_add_prod(sh, sl, h0, l0, v0);
+    df_add_prod(sh, sl, h1, l1, v1);
+    df_add_prod(sh, sl, h2, l2, v2);
+    df_add_prod(sh, sl, h3, l3, v3);
+  }
+  for (; j < n; j += 32) df_add_prod(sh, sl, h[j], l[j], r[j]);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, sh, off);
+    const float ol = __shfl_xor_sync(0xffffffffu, sl, off);
+    df_add(sh, sl, oh, ol);
+  }
+  if (lane == 0) x[row] = __fadd_rn(sh, sl);
 }
 
 template <class X>
@@ -464,6 +557,18 @@ void dense_gemv(const afp_context* ctx, int64_t n, const X* Ainv, const X* r, X*
   check_launch(ctx, "dense gemv");
 }
 
+void split_df(const afp_context* ctx, int64_t n2, const double* inv, float* hi, float* lo) {
+  if (n2 == 0) return;
+  k_split_df<<<grid_for(n2, BLK), BLK, 0, ctx->stream>>>(n2, inv, hi, lo);
+  check_launch(ctx, "double-float split");
+}
+
+void dense_gemv_df(const afp_context* ctx, int64_t n, const float* hi, const float* lo, const float* r, float* x) {
+  if (n == 0) return;
+  launch_pdl(ctx->stream, grid_for(n * 32, BLK), BLK, 0, k_dense_gemv_df, n, hi, lo, r, x);
+  check_launch(ctx, "dense gemv (double-float)");
+}
+
 template <class X>
 void diag_solve(const afp_context* ctx, const CSRView<X>& A, const X* r, X* x) {
   launch_pdl(ctx->stream, grid_for(A.m, BLK), BLK, 0, k_diag_solve<X>, A.m, A.rowptr, A.vals, r, x);
@@ -574,8 +679,12 @@ bool dense_inverse(const afp_context* ctx, const CSRView<double>& A, double* inv
 
 void csr_spmv(const afp_context* ctx, int64_t m, const int* rowptr, const int* cols, const double* vals,
               const double* x, double* y) {
-  CSRView<double> A{m, rowptr, cols, vals, 8};
-  spmv<double, double>(ctx, A, x, y, false);
+  // A plain launch, without the PDL attribute: k_spmv loads the matrix before
+  // griddepcontrol.wait, and the caller's preceding kernel on this stream
+  // (assembly, Dirichlet rows, a value upload) may be the one writing it.
+  if (m == 0) return;
+  k_spmv<8, double, double, false><<<grid_for(m * 8, BLK), BLK, 0, ctx->stream>>>(m, rowptr, cols, vals, x, y);
+  check_launch(ctx, "spmv");
 }
 
 // explicit instantiations
