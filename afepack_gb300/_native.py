@@ -98,6 +98,7 @@ SIGNATURES = {
     "afp_matrix_set_values": [C.c_void_p, C.c_void_p],
     "afp_matrix_download": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
     "afp_matrix_vmult": [C.c_void_p, C.c_void_p, C.c_void_p],
+    "afp_matrix_vmult_noalloc": [C.c_void_p, C.c_void_p, C.c_void_p],
     "afp_matrix_destroy": [C.c_void_p],
     "afp_apply_dirichlet": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],
     "afp_amg_default_opts": [C.POINTER(AMGOpts)],

@@ -28,6 +28,7 @@ SOURCES = [
     ("solve.cu", []),
     ("amg.cu", []),
     ("mrhs.cu", []),
+    ("noalloc.cu", []),
     ("coarsen_host.cpp", []),
     ("server.cpp", []),
 ]

@@ -108,6 +108,19 @@ afp_status afp_matrix_set_values(afp_matrix *a, const double *vals);
 afp_status afp_matrix_download(const afp_matrix *a, int32_t *rowptr, int32_t *cols, double *vals);
 /* y = A x  (SparseMatrix::vmult, include/AFEPack/SparseMatrix.h:100-114) */
 afp_status afp_matrix_vmult(afp_matrix *a, const double *x, double *y);
+/* y = A x without allocating device memory.  No counterpart in the
+ * reference: it exists for callers that cannot let a library allocate on the
+ * device when they call it (device memory already reserved by their own
+ * arena, a hard device-memory cap, or a time-step loop whose allocator must
+ * not grow).  x and y are staged in a fixed static device array of
+ * 2 x AFP_NOALLOC_MAX_ENTRIES doubles (32 MiB, held by every GPU that loads
+ * the library), so matrices with more rows or columns than that are refused
+ * with AFP_ERR_UNSUPPORTED.  All calls share the array: calls whose GPU work
+ * overlaps race.  Nothing in it needs to start at zero.  The first call on a
+ * device looks up the array's device address; make it before any stream
+ * capture. */
+#define AFP_NOALLOC_MAX_ENTRIES (1 << 21)
+afp_status afp_matrix_vmult_noalloc(afp_matrix *a, const double *x, double *y);
 afp_status afp_matrix_destroy(afp_matrix *a);
 
 /* BoundaryConditionAdmin::apply(A, u, f, preserve_symmetry)
