@@ -36,7 +36,8 @@ class AMGOpts(C.Structure):
     _fields_ = [("tolerance", C.c_double), ("smooth_step", C.c_int), ("max_coarse", C.c_int),
                 ("min_density", C.c_double), ("alpha", C.c_double), ("precision", C.c_int),
                 ("dense_tail", C.c_int), ("max_colors", C.c_int), ("symmetric", C.c_int),
-                ("coarse_colors", C.c_int), ("interp_bf16", C.c_int)]
+                ("coarse_colors", C.c_int), ("interp_bf16", C.c_int),
+                ("fused_vcycle", C.c_int)]
 
 
 class SolveInfo(C.Structure):

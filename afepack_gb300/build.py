@@ -28,6 +28,7 @@ SOURCES = [
     ("solve.cu", []),
     ("amg.cu", []),
     ("mrhs.cu", []),
+    ("vcycle_fused.cu", []),
     ("noalloc.cu", []),
     ("coarsen_host.cpp", []),
     ("server.cpp", []),

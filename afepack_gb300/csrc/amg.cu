@@ -148,10 +148,39 @@ void vcycle(afp_amg* h, X* x0, const X* r0, bool zero_init) {
   }
 }
 
-// Mixed-precision V-cycle: FP32 levels, P / P^T in BF16 or FP32 (opts.interp_bf16).
+// Mixed-precision V-cycle: FP32 levels, P / P^T in BF16 or FP32 (opts.interp_bf16);
+// one cooperative kernel when the fused plan exists, else the launch chain.
 void vcycle_mixed(afp_amg* h, float* x0, const float* r0) {
-  if (h->opts.interp_bf16) vcycle<float, __nv_bfloat16>(h, x0, r0, true);
+  if (h->fused) fused_vcycle(h, x0, r0);
+  else if (h->opts.interp_bf16) vcycle<float, __nv_bfloat16>(h, x0, r0, true);
   else vcycle<float, float>(h, x0, r0, true);
+}
+
+// Runs a graph build; if it fails while the fused V-cycle is in use (a graph
+// that cannot hold a cooperative kernel), drops the fused plan and retries
+// with the launch chain.
+void drop_fused(afp_amg* h) {
+  // graphs captured with the fused kernel refer to the plan's buffers
+  if (h->graph32) cudaGraphExecDestroy(h->graph32);
+  if (h->loop32) cudaGraphExecDestroy(h->loop32);
+  h->graph32 = h->loop32 = nullptr;
+  h->fused.reset();
+}
+
+template <class F>
+void with_chain_fallback(afp_amg* h, F&& build) {
+  try {
+    build();
+  } catch (const Error&) {
+    if (!h->fused) throw;
+    cudaGetLastError();
+    drop_fused(h);
+    build();
+  }
+}
+
+void check_fused(afp_amg* h) {
+  if (fused_timed_out(h)) fail(AFP_ERR_TIMEOUT, "fused V-cycle: a grid barrier wait ran out");
 }
 
 // Captures (once) and replays the preconditioner z = V(r) on the solver's
@@ -162,21 +191,28 @@ void precondition(afp_amg* h) {
   cudaGraphExec_t& exec = mixed ? h->graph32 : h->graph64;
   int64_t& nodes = mixed ? h->graph32_nodes : h->graph64_nodes;
   if (exec == nullptr) {
-    cudaGraph_t g;
-    const int64_t before = ctx->launches.n;
-    AFP_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    try {
-      if (mixed) vcycle_mixed(h, h->z32.get(), h->r32.get());
-      else vcycle<double, double>(h, h->z.get(), h->r.get(), true);
-    } catch (...) {
-      cudaStreamEndCapture(ctx->stream, &g);
-      throw;
-    }
-    AFP_CUDA(cudaStreamEndCapture(ctx->stream, &g));
-    AFP_CUDA(cudaGraphInstantiate(&exec, g, 0));
-    AFP_CUDA(cudaGraphDestroy(g));
-    nodes = ctx->launches.n - before;
-    ctx->launches.n = before;
+    with_chain_fallback(h, [&] {
+      cudaGraph_t g = nullptr;
+      const int64_t before = ctx->launches.n;
+      AFP_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        if (mixed) vcycle_mixed(h, h->z32.get(), h->r32.get());
+        else vcycle<double, double>(h, h->z.get(), h->r.get(), true);
+      } catch (...) {
+        cudaStreamEndCapture(ctx->stream, &g);
+        if (g) cudaGraphDestroy(g);
+        ctx->launches.n = before;
+        throw;
+      }
+      const int64_t captured = ctx->launches.n - before;
+      ctx->launches.n = before;
+      AFP_CUDA(cudaStreamEndCapture(ctx->stream, &g));
+      const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) exec = nullptr;
+      AFP_CUDA(ie);
+      nodes = captured;
+    });
   }
   if (mixed) convert<double, float>(ctx, h->lv[0].n, h->r.get(), h->r32.get());
   AFP_CUDA(cudaGraphLaunch(exec, ctx->stream));
@@ -365,6 +401,9 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
     h->z32.alloc(ctx, n0);
   }
   sync(ctx);
+  static const bool no_fused = std::getenv("AFP_NO_FUSED") != nullptr;  // A/B timing of the launch chain
+  if (mixed && h->opts.fused_vcycle && !no_fused) fused_build(h);
+  else h->fused.reset();
 }
 
 void setup(afp_amg* h, afp_matrix* A, bool lazy) {
@@ -462,9 +501,12 @@ void lazy_reinit(afp_amg* h, afp_matrix* A) {
     dc.va = std::move(cvals);
     refDev.push_back(std::move(dc));
   }
+  // every captured graph refers to the level buffers rebuilt below
   if (h->graph64) cudaGraphExecDestroy(h->graph64);
   if (h->graph32) cudaGraphExecDestroy(h->graph32);
-  h->graph64 = h->graph32 = nullptr;
+  if (h->loop64) cudaGraphExecDestroy(h->loop64);
+  if (h->loop32) cudaGraphExecDestroy(h->loop32);
+  h->graph64 = h->graph32 = h->loop64 = h->loop32 = nullptr;
   h->multi.reset();
   h->lv.clear();
   build_solve_layout(h, refDev, A);
@@ -607,7 +649,8 @@ void pcg(afp_amg* h, double* x_user, const double* b_user, double tol, int maxit
   static const bool host_loop = std::getenv("AFP_HOST_LOOP") != nullptr;
   if (!conv && maxit > 0 && !host_loop) {
     const int pi = h->opts.precision == AFP_PRECISION_MIXED ? 1 : 0;
-    cudaGraphExec_t exec = loop_graph(h);
+    cudaGraphExec_t exec = nullptr;
+    with_chain_fallback(h, [&] { exec = loop_graph(h); });
     ctx->h_scalars[0] = tol * tol * hs[4];
     copy(ctx, s + 6, ctx->h_scalars, sizeof(double));
     int lv[2] = {0, maxit};
@@ -650,6 +693,7 @@ void pcg(afp_amg* h, double* x_user, const double* b_user, double tol, int maxit
   AFP_CUDA(cudaEventRecord(e1, ctx->stream));
   copy(ctx, x_user, h->tmp.get(), sizeof(double) * n);
   sync(ctx);
+  check_fused(h);
   float ms = 0;
   AFP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
   cudaEventDestroy(e0);
@@ -681,6 +725,7 @@ void afp_amg_default_opts(afp_amg_opts* o) {
   o->symmetric = 1;
   o->coarse_colors = 8;
   o->interp_bf16 = 0;
+  o->fused_vcycle = 1;
 }
 
 afp_status afp_amg_setup(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out) {
@@ -799,6 +844,7 @@ afp_status afp_amg_solve(afp_amg* h, double* x, const double* r, double tol, int
     AFP_CUDA(cudaEventRecord(e1, ctx->stream));
     copy(ctx, x, h->tmp.get(), sizeof(double) * n);
     sync(ctx);
+    check_fused(h);
     float ms = 0;
     AFP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);
@@ -873,6 +919,7 @@ afp_status afp_amg_time_kernel(afp_amg* h, int kind, int level, int reps, double
     for (int i = 0; i < reps; ++i) unit();
     AFP_CUDA(cudaEventRecord(e1, ctx->stream));
     sync(ctx);
+    check_fused(h);
     float t = 0;
     AFP_CUDA(cudaEventElapsedTime(&t, e0, e1));
     cudaEventDestroy(e0);
@@ -883,7 +930,7 @@ afp_status afp_amg_time_kernel(afp_amg* h, int kind, int level, int reps, double
     else if (kind == 1) *bytes = mat + 3.0 * n * v;      // read x, r, write out
     else if (kind == 3) *bytes = (double)h->lv[0].nnz * 12 + 4.0 * (h->lv[0].n + 1) + 2.0 * h->lv[0].n * 8;
     else {
-      const double s = h->opts.smooth_step, vp = mixed ? 2.0 : 8.0;
+      const double s = h->opts.smooth_step, vp = mixed ? (h->opts.interp_bf16 ? 2.0 : 4.0) : 8.0;
       double b = 0;
       for (int l = 0; l < h->t; ++l) {
         const Level& Q = h->lv[l];
@@ -893,7 +940,7 @@ afp_status afp_amg_time_kernel(afp_amg* h, int kind, int level, int reps, double
              2.0 * h->lv[l + 1].n * v;
       }
       const double nt = (double)h->lv[h->t].n;
-      b += h->tail_dense ? nt * nt * v : 0.0;
+      b += h->tail_dense ? nt * nt * 8.0 : 0.0;  // FP64 inverse, or its FP32 hi + lo pair
       *bytes = b;
     }
   });

@@ -77,6 +77,49 @@ struct MultiState {
   }
 };
 
+// Device-side description of the FP32 V-cycle for the fused cooperative
+// kernel (vcycle_fused.cu): one entry per smoothed level plus the tail level.
+struct FusedLevel {
+  int64_t n = 0;
+  const int* rp = nullptr;
+  const int* ci = nullptr;
+  const float* va = nullptr;
+  int vec = 32;
+  const float* l1d = nullptr;  // l1 diagonal of the overflow class
+  float* x = nullptr;          // level vectors (level 0 uses the launch's x0 / r0)
+  float* r = nullptr;
+  float* tmp = nullptr;
+  const int* prp = nullptr;    // restriction P (rows = next level)
+  const int* pci = nullptr;
+  const float* pva = nullptr;
+  int pvec = 32;
+  const int* trp = nullptr;    // prolongation P^T (rows = this level)
+  const int* tci = nullptr;
+  const float* tva = nullptr;
+  int tvec = 32;
+};
+struct FusedPhase {
+  int op;
+  int level;
+  int64_t r0, r1;
+};
+struct FusedTail {
+  int64_t n;
+  int level;
+  const float* hi;
+  const float* lo;
+  float* x;
+  const float* r;
+};
+struct FusedPlan {
+  DevBuf<FusedLevel> levels;
+  DevBuf<FusedPhase> phases;
+  int nphase = 0;
+  FusedTail tail{};
+  DevBuf<unsigned> bar;  // [arrivals, generation, error word, unused]
+  int64_t grid = 0;
+};
+
 }  // namespace afp
 
 struct afp_amg {
@@ -103,6 +146,7 @@ struct afp_amg {
   cudaGraphExec_t loop64 = nullptr, loop32 = nullptr;
   int64_t loop_pre_nodes[2] = {0, 0}, loop_body_nodes[2] = {0, 0};
   afp::DevBuf<int> loopvars;  // [iterations done, iteration limit]
+  std::unique_ptr<afp::FusedPlan> fused;  // set when the FP32 V-cycle runs as one cooperative kernel
 
   ~afp_amg() {
     if (graph64) cudaGraphExecDestroy(graph64);
@@ -116,4 +160,9 @@ namespace afp {
 // Batched CG over nrhs columns (mrhs.cu).
 void pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, double tol, int maxit,
                afp_solve_info* info);
+// Fused FP32 V-cycle (vcycle_fused.cu): plan from the solve layout (leaves
+// h->fused empty when it does not apply), launch, and the barrier-timeout flag.
+void fused_build(afp_amg* h);
+void fused_vcycle(afp_amg* h, float* x0, const float* r0);
+bool fused_timed_out(afp_amg* h);
 }  // namespace afp

@@ -110,6 +110,7 @@ afp_status run(afp_context* ctx, Job& j, const afp_server_opts& o) {
   AFP_TRY(afp_apply_dirichlet(K, b.data(), j.dirichlet.data(), nullptr, 1));
   afp_amg_opts mo;
   afp_amg_default_opts(&mo);
+  mo.fused_vcycle = 0;  // workers solve concurrently: no grid-wide cooperative kernels
   mo.precision = o.precision;
   if (o.dense_tail >= 0) mo.dense_tail = o.dense_tail;
   AFP_TRY(afp_amg_setup(K, &mo, &amg));

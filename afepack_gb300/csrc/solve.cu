@@ -19,13 +19,15 @@
 namespace afp {
 
 // Lanes per row: the smallest power of two in [4, 32] with at most
-// `entries per lane` (default 1; AFP_ENTRIES_PER_LANE overrides it for
-// tuning) of the level's mean row length on each lane.
+// `entries per lane` of the level's mean row length on each lane.  Four per
+// lane (AFP_ENTRIES_PER_LANE overrides it for tuning) measured fastest on the
+// 64^3 P1 level 0 (15 entries per row, 4 lanes): its FP32 Gauss-Seidel sweep
+// 20 us against 32 us with one entry per lane, the residual 7 us against 19.
 int pick_vec(double avg) {
   static const double epl = [] {
     const char* e = std::getenv("AFP_ENTRIES_PER_LANE");
     const double v = e ? std::atof(e) : 0.0;
-    return v > 0.0 ? v : 1.0;
+    return v > 0.0 ? v : 4.0;
   }();
   int vec = 4;
   while (vec < 32 && vec * epl < avg) vec *= 2;
@@ -77,14 +79,18 @@ __device__ __forceinline__ T group_sum(T s) {
 // this overlaps two of the three dependent memory round trips of a row with
 // the predecessor's drain.  The products are summed in the same order as a
 // plain k = begin + lane, begin + lane + VEC, ... loop.
-template <int VEC>
+// Pairs loaded ahead per lane.  FP64 keeps it short: each guarded product
+// of the unrolled loop costs an FP64 instruction slot whether or not the
+// entry exists, and FP64 instruction throughput is what bounds the FP64
+// kernels on this GPU.
+template <int VEC, class V>
 constexpr int prefetch_depth() {
-  return VEC >= 32 ? 8 : 4;
+  return sizeof(V) == 8 ? (VEC >= 32 ? 2 : 1) : (VEC >= 32 ? 8 : 4);
 }
 
 template <int VEC, class V>
 struct RowAhead {
-  static constexpr int PF = prefetch_depth<VEC>();
+  static constexpr int PF = prefetch_depth<VEC, V>();
   int k, e;  // first entry of this lane, row end
   int c[PF];
   V v[PF];

@@ -134,7 +134,7 @@ afp_status afp_apply_dirichlet(afp_matrix *a, double *f, const int32_t *dirichle
 /* ------------------------------------------------------------------ AMG */
 typedef enum afp_precision {
   AFP_PRECISION_FP64 = 0,   /* V-cycle in FP64                                   */
-  AFP_PRECISION_MIXED = 1   /* V-cycle in FP32 (BF16 P/P^T), FP64 outer recurrences */
+  AFP_PRECISION_MIXED = 1   /* V-cycle in FP32, FP64 outer recurrences           */
 } afp_precision;
 
 typedef struct afp_amg_opts {
@@ -157,6 +157,13 @@ typedef struct afp_amg_opts {
   int interp_bf16;      /* mixed precision only: keep P and P^T in BF16 (1) or
                            in FP32 (0, default: BF16 interpolation weights cost
                            the 3D P1 solve about 1.5x the PCG iterations)       */
+  int fused_vcycle;     /* mixed precision: run each V-cycle as one cooperative
+                           kernel with grid barriers instead of a chain of
+                           ~150-200 launches (1, default; falls back to the
+                           chain where a graph cannot hold it).  Two such
+                           kernels running at once on one GPU compete for its
+                           SMs, so solvers used concurrently (the server's
+                           workers) set 0                                      */
 } afp_amg_opts;
 
 typedef struct afp_solve_info {

@@ -152,6 +152,48 @@ def test_pcg_mixed_3d_hierarchy_keeps_fp64_iterations(ctx):
     assert it[1] <= it[0] + 2, it
 
 
+def test_fused_vcycle_matches_launch_chain(ctx):
+    """The FP32 V-cycle as one cooperative kernel does the launch chain's
+    arithmetic in the same order: same iterates bit for bit, with a small
+    fraction of the launches."""
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import MIXED, AMGSolver
+    wl = W.poisson3d_p1(32)
+    _, K, b = system(ctx, wl)
+    runs = {}
+    for name, fused in (("chain", False), ("fused", True)):
+        amg = AMGSolver(K, precision=MIXED, fused_vcycle=fused)
+        x = np.zeros_like(b)
+        n0 = ctx.launch_count()
+        amg.solve(x, b, 0.0, 2)  # three V-cycles
+        launches = ctx.launch_count() - n0
+        xp, info = amg.pcg(b, 1e-10, 300)
+        runs[name] = (x, launches, xp, info["iterations"])
+    assert runs["fused"][1] * 5 < runs["chain"][1], (runs["fused"][1], runs["chain"][1])
+    assert np.array_equal(runs["fused"][0], runs["chain"][0])
+    assert runs["fused"][3] == runs["chain"][3]
+    assert np.array_equal(runs["fused"][2], runs["chain"][2])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_pcg_after_lazy_reinit_uses_new_values(ctx, precision):
+    """lazyReinit on the same pattern rebuilds every level; a PCG solve after
+    it (its whole-loop graph included) must use the new values."""
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import AMGSolver
+    wl = W.poisson2d_p1(64)
+    _, K, b = system(ctx, wl)
+    amg = AMGSolver(precision=precision)
+    amg.lazyReinit(K)
+    x1, info1 = amg.pcg(b, 1e-10, 300)
+    assert info1["converged"]
+    K.set_values(K.values() * 1.5)  # same pattern object, new values: A' = 1.5 A
+    amg.lazyReinit(K)
+    x2, info2 = amg.pcg(b, 1e-10, 300)
+    assert info2["converged"]
+    assert np.linalg.norm(x2 - x1 / 1.5) <= 1e-8 * np.linalg.norm(x1)
+
+
 def test_multi_rhs_matches_single(ctx):
     from afepack_gb300 import workloads as W
     from afepack_gb300.amg import AMGSolver
