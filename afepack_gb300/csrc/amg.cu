@@ -725,7 +725,7 @@ void afp_amg_default_opts(afp_amg_opts* o) {
   o->symmetric = 1;
   o->coarse_colors = 8;
   o->interp_bf16 = 0;
-  o->fused_vcycle = 1;
+  o->fused_vcycle = 0;
 }
 
 afp_status afp_amg_setup(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out) {

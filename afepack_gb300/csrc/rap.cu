@@ -12,7 +12,9 @@
 // distinct, so every output entry receives its products in exactly the
 // reference's order: row_entry[c] += P(i,a)*A(a,b)*Pt(b,c).  Compiled with
 // -fmad=false, the result is bitwise that of getPMPt.
+#include <algorithm>
 #include <climits>
+#include <vector>
 
 #include "common.cuh"
 #include "kernels.cuh"
@@ -22,7 +24,7 @@ namespace {
 
 constexpr int WARP_CAP = 1024;      // hash slots of the warp-level symbolic pass
 constexpr int BLOCK_CAP = 16384;    // hash slots of the block-level pass (2 x 64 KB of shared memory)
-constexpr int ACC_CAP = 1024;       // row length kept in shared memory by the numeric pass
+constexpr size_t NUM_SMEM_MAX = 200 * 1024;  // shared memory the numeric pass may use per block
 
 __device__ __forceinline__ unsigned hash_slot(int key, int cap) {
   return ((unsigned)key * 2654435761u) & (unsigned)(cap - 1);
@@ -194,18 +196,23 @@ __device__ __forceinline__ int find_slot(const int* c, int R, int key, int row) 
 }
 
 // Numeric pass: exact reference accumulation order (see file comment).
+// Rows of up to acc_cap entries accumulate in the warp's slice of shared
+// memory (their column list too, for the slot searches); longer rows in
+// place in global memory.  acc_cap is sized by the host from the product's
+// longest row, so the nearly dense coarse levels of 3D hierarchies stay in
+// shared memory as well.
 __global__ void k_rap_numeric(int64_t n_c, const int* __restrict__ prp, const int* __restrict__ pc,
                               const double* __restrict__ pv, const int* __restrict__ arp, const int* __restrict__ ac,
                               const double* __restrict__ av, const int* __restrict__ trp, const int* __restrict__ tc,
                               const double* __restrict__ tv, const int* __restrict__ rowptr,
-                              const int* __restrict__ cols, double* __restrict__ vals) {
+                              const int* __restrict__ cols, double* __restrict__ vals, int acc_cap) {
   extern __shared__ __align__(16) unsigned char sm_num[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-  double* sacc = reinterpret_cast<double*>(sm_num) + (size_t)warp * ACC_CAP;
-  int* scol = reinterpret_cast<int*>(reinterpret_cast<double*>(sm_num) + (size_t)wpb * ACC_CAP) + warp * ACC_CAP;
+  double* sacc = reinterpret_cast<double*>(sm_num) + (size_t)warp * acc_cap;
+  int* scol = reinterpret_cast<int*>(reinterpret_cast<double*>(sm_num) + (size_t)wpb * acc_cap) + warp * acc_cap;
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < n_c; i += (int64_t)gridDim.x * wpb) {
     const int r0 = rowptr[i], R = rowptr[i + 1] - r0;
-    const bool in_smem = R <= ACC_CAP;
+    const bool in_smem = R <= acc_cap;
     double* acc = in_smem ? sacc : vals + r0;
     const int* rc = in_smem ? scol : cols + r0;
     for (int t = lane; t < R; t += 32) {
@@ -284,10 +291,25 @@ void galerkin_product(const afp_context* ctx, int64_t n_c, int64_t n_f, const in
                                                                out.rowptr.get(), out.cols.get(), big_flag.get());
   check_launch(ctx, "rap symbolic fill");
   vals.alloc(ctx, out.nnz);
-  const size_t smem_n = (size_t)wpb * ACC_CAP * (sizeof(double) + sizeof(int));
+  // shared-memory accumulator per warp: the longest row (at least 1024
+  // entries), with fewer warps per block when rows are long
+  int rmax = 0;
+  {
+    std::vector<int> rp(n_c + 1);
+    out.rowptr.download(rp.data(), n_c + 1);
+    sync(ctx);
+    for (int64_t i = 0; i < n_c; ++i) rmax = std::max(rmax, rp[i + 1] - rp[i]);
+  }
+  const size_t per_entry = sizeof(double) + sizeof(int);
+  int acc_cap = std::max(1024, (rmax + 31) / 32 * 32);
+  int wpn = 4;
+  while (wpn > 1 && (size_t)wpn * acc_cap * per_entry > NUM_SMEM_MAX) --wpn;
+  if ((size_t)acc_cap * per_entry > NUM_SMEM_MAX) acc_cap = (int)(NUM_SMEM_MAX / per_entry) / 32 * 32;  // global
+  const size_t smem_n = (size_t)wpn * acc_cap * per_entry;
+  const unsigned grid_n = (unsigned)std::min<int64_t>((n_c + wpn - 1) / wpn, (int64_t)ctx->sm_count * 16);
   AFP_CUDA(cudaFuncSetAttribute(k_rap_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_n));
-  k_rap_numeric<<<grid, wpb * 32, smem_n, ctx->stream>>>(n_c, prp, pc, pv, arp, ac, av, trp, tc, tv, out.rowptr.get(),
-                                                         out.cols.get(), vals.get());
+  k_rap_numeric<<<grid_n, wpn * 32, smem_n, ctx->stream>>>(n_c, prp, pc, pv, arp, ac, av, trp, tc, tv,
+                                                           out.rowptr.get(), out.cols.get(), vals.get(), acc_cap);
   check_launch(ctx, "rap numeric");
 }
 

@@ -47,18 +47,30 @@ __device__ __forceinline__ unsigned long long now_ns() {
   return t;
 }
 
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+__device__ __forceinline__ void red_add_release(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // Sense-by-generation grid barrier: bar[0] arrivals, bar[1] generation,
-// bar[2] error word.  Returns false (for every thread of the block) once the
-// error word is set.
+// bar[2] error word.  Ordering comes from the atomics themselves: thread 0
+// arrives with an acquire-release add after the block's bar.sync (its
+// release covers the block's writes), the last arriver resets the count and
+// publishes the next generation with a release add, and the others wait on
+// it with acquire loads -- no separate sequentially consistent fences.
+// Returns false (for every thread of the block) once the error word is set.
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, unsigned& gen, int* s_ok) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned arrived = atomicAdd(&bar[0], 1u);
+    const unsigned arrived = atom_add_acq_rel(&bar[0], 1u);
     if (arrived == nblocks - 1) {
       atomicExch(&bar[0], 0u);
-      __threadfence();
-      atomicAdd(&bar[1], 1u);
+      red_add_release(&bar[1], 1u);
     } else {
       const unsigned long long t0 = now_ns();
       unsigned spins = 0;
@@ -72,7 +84,6 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, un
         }
       }
     }
-    __threadfence();
     *s_ok = ld_acquire(&bar[2]) == 0u;
   }
   ++gen;

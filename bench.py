@@ -127,6 +127,14 @@ def run_ours(args):
     from afepack_gb300.amg import FP64, MIXED, AMGSolver
     from afepack_gb300.fem import BoundaryConditionAdmin, Context, Space, assemble
 
+    clock = [time.perf_counter()]
+
+    def phase(name):
+        # wall time of each part of the run, on stderr (the JSON line is stdout)
+        now = time.perf_counter()
+        print(f"[bench] {name}: {now - clock[0]:.1f} s", file=sys.stderr, flush=True)
+        clock[0] = now
+
     B.build()
     torch.cuda.init()
     dev = torch.device("cuda:0")
@@ -170,6 +178,7 @@ def run_ours(args):
     levels = [amg64.level_info(l) for l in range(amg64.solve_levels())]
 
     # ---- FP64 reference solution (tight) for the error of the timed solves
+    phase("setup")
     x_ref, info_ref = amg64.pcg(b, 1e-14, 1000)
     torch.cuda.synchronize()
 
@@ -177,6 +186,7 @@ def run_ours(args):
         x = torch.zeros_like(b)
         return x, amg.pcg(b, tol, 1000, x)[1]
 
+    phase("fp64 reference solution")
     results = {}
     clocks = Clocks()
     for name, amg in (("fp64", amg64), ("mixed", amg32)):
@@ -207,6 +217,7 @@ def run_ours(args):
                          "p50_ms": float(np.percentile(t, 50)), "p99_ms": float(np.percentile(t, 99)),
                          "pcg_iterations": int(np.median(iters)), "rel_err_vs_fp64": err}
 
+    phase("timed solves")
     # ---- end to end through the C ABI with host buffers (H2D of b, D2H of x inside)
     b_host = b.cpu().numpy().copy()
     bh = torch.from_numpy(b_host).pin_memory()
@@ -225,6 +236,7 @@ def run_ours(args):
             e2e_t.append(s0.elapsed_time(s1))
     e2e_t = np.array(e2e_t)
 
+    phase("e2e")
     # ---- roofline: kernels timed live with CUDA events on the library stream
     peaks = {}
     try:
@@ -256,11 +268,14 @@ def run_ours(args):
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800 GB/s",
             "kernels": kernels}
 
+    phase("kernel timings")
     launches = ctx.launch_count()
     # CPU baseline (rank 0, N=1): the reference algorithm's solve on one core
     amg_full = AMGSolver(K, precision=FP64, dense_tail=0)
+    phase("full-depth hierarchy for the CPU sample")
     cpu = cpu_baseline_sample(amg_full, b.cpu().numpy().copy(), args.tol)
     del amg_full
+    phase("CPU sample")
     line = {
         "metric": METRIC, "value": round(results["mixed"]["solves_per_s"], 3), "unit": "solves/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,

@@ -159,11 +159,13 @@ typedef struct afp_amg_opts {
                            the 3D P1 solve about 1.5x the PCG iterations)       */
   int fused_vcycle;     /* mixed precision: run each V-cycle as one cooperative
                            kernel with grid barriers instead of a chain of
-                           ~150-200 launches (1, default; falls back to the
-                           chain where a graph cannot hold it).  Two such
-                           kernels running at once on one GPU compete for its
-                           SMs, so solvers used concurrently (the server's
-                           workers) set 0                                      */
+                           ~150-200 PDL launches (1), or as the chain (0,
+                           default: on GB300 a grid barrier measured ~4-5 us,
+                           more than a chained launch, so the chain is faster:
+                           1.03 ms vs 1.71 ms per 64^3 P1 V-cycle).  Both give
+                           the same iterates bit for bit.  Two such kernels
+                           running at once on one GPU compete for its SMs, so
+                           the server's concurrent workers never use it. */
 } afp_amg_opts;
 
 typedef struct afp_solve_info {
