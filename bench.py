@@ -107,6 +107,16 @@ class Clocks:
                 "samples": len(sm)}
 
 
+_CLOCK = [time.perf_counter()]
+
+
+def phase(name):
+    """Wall time of each part of a run, on stderr (the JSON line is stdout)."""
+    now = time.perf_counter()
+    print(f"[bench] {name}: {now - _CLOCK[0]:.1f} s", file=sys.stderr, flush=True)
+    _CLOCK[0] = now
+
+
 def profiled_traffic(workload):
     """DRAM bytes (read + write) of one fused V-cycle launch from the committed
     ncu summary of this workload, or None when there is none."""
@@ -126,14 +136,6 @@ def run_ours(args):
     from afepack_gb300 import workloads as W
     from afepack_gb300.amg import FP64, MIXED, AMGSolver
     from afepack_gb300.fem import BoundaryConditionAdmin, Context, Space, assemble
-
-    clock = [time.perf_counter()]
-
-    def phase(name):
-        # wall time of each part of the run, on stderr (the JSON line is stdout)
-        now = time.perf_counter()
-        print(f"[bench] {name}: {now - clock[0]:.1f} s", file=sys.stderr, flush=True)
-        clock[0] = now
 
     B.build()
     torch.cuda.init()
@@ -271,10 +273,7 @@ def run_ours(args):
     phase("kernel timings")
     launches = ctx.launch_count()
     # CPU baseline (rank 0, N=1): the reference algorithm's solve on one core
-    amg_full = AMGSolver(K, precision=FP64, dense_tail=0)
-    phase("full-depth hierarchy for the CPU sample")
-    cpu = cpu_baseline_sample(amg_full, b.cpu().numpy().copy(), args.tol)
-    del amg_full
+    cpu = cpu_baseline_sample(amg64, b.cpu().numpy().copy(), args.tol)
     phase("CPU sample")
     line = {
         "metric": METRIC, "value": round(results["mixed"]["solves_per_s"], 3), "unit": "solves/s",
@@ -321,9 +320,12 @@ def run_multi(args):
     bca.apply(K, np.ascontiguousarray(Bm[:, 0]).copy())
     Bm[d != 0] = 0.0
     t1 = time.perf_counter()
+    phase("multi: assembly and right-hand sides")
     amg32 = AMGSolver(K, precision=MIXED)
     t2 = time.perf_counter()
+    phase("multi: mixed setup")
     amg64 = AMGSolver(K, precision=FP64)
+    phase("multi: fp64 setup")
     Bd = torch.from_numpy(np.ascontiguousarray(Bm)).to(dev)
 
     def ev():
@@ -331,8 +333,10 @@ def run_multi(args):
 
     # FP64 references for the error: FP64 CG to 1e-13 on a few columns
     refs = {c: amg64.pcg(np.ascontiguousarray(Bm[:, c]), 1e-13, 1000)[0] for c in (0, args.nrhs - 1)}
+    phase("multi: fp64 references")
     for _ in range(max(args.warmup, 3)):
         amg32.pcg_multi(Bd, args.tol_multi, 500)
+    phase("multi: warm-up")
     times = []
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
@@ -343,6 +347,7 @@ def run_multi(args):
         s1.record(stream)
         torch.cuda.synchronize()
         times.append(s0.elapsed_time(s1))
+    phase("multi: timed batches")
     Xh = X.cpu().numpy()
     err = max(np.linalg.norm(Xh[:, c] - r) / np.linalg.norm(r) for c, r in refs.items())
     # drop-in: sequential FP64 single solves (a bounded sample of the 64)
@@ -382,6 +387,7 @@ def run_stream(args):
     t0 = time.perf_counter()
     wls = [W.request_workload(r) for r in reqs]
     gen_s = time.perf_counter() - t0
+    phase("stream: request generation")
     out = {}
     for name, prec in (("mixed", 1), ("fp64", 0)):
         with Server(workers=args.workers, precision=prec, tol=args.tol) as srv:
@@ -394,6 +400,7 @@ def run_stream(args):
             res = [srv.wait(t)[1] for t in tickets]
             wall = time.perf_counter() - s0
             st = srv.stats()
+            phase(f"stream: {name} server run")
         lat = np.array([r["latency_seconds"] for r in res])
         out[name] = {"solves_per_s": len(res) / wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
                      "p99_ms": 1e3 * float(np.percentile(lat, 99)), "failed": int(st["failed"]),
@@ -499,21 +506,28 @@ def run_reference(args):
 
 
 def cpu_baseline_sample(amg_gpu, b_host, tol):
-    """One single-threaded oracle CG solve on the hierarchy the GPU built at the
-    reference's full depth (bitwise the reference's, which the tests check)."""
+    """One single-threaded oracle CG solve (the reference's CG shape, one
+    reference V-cycle per iteration: lexicographic Gauss-Seidel, restriction,
+    prolongation) on the hierarchy the GPU built -- levels bitwise the
+    reference's down to the dense tail -- with the reference's coarsest
+    treatment, an explicit inverse, applied at that tail level (inverted here
+    with LAPACK; the reference would keep coarsening it on the host for
+    minutes)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     nl = amg_gpu.n_project()
     A = [O.CSR(*amg_gpu.level_matrix(l), (amg_gpu.level_info(l)[0],) * 2) for l in range(nl + 1)]
     P = [O.CSR(*amg_gpu.projection(l), (amg_gpu.level_info(l + 1)[0], amg_gpu.level_info(l)[0])) for l in range(nl)]
-    amg = O.AMG.from_levels(A, P)
+    inv = np.linalg.inv(A[-1].to_scipy().toarray())
+    amg = O.AMG.from_levels(A, P, coarse_inv=inv)
     t0 = time.perf_counter()
     x, it, rel = amg.pcg(b_host, tol, 1000)
     dt = time.perf_counter() - t0
     return {"value": round(1.0 / dt, 4), "unit": "solves/s", "cores": 1, "kind": "port",
-            "sample": f"one CG solve of the same system ({it} iterations, one reference V-cycle each) on 1 core; "
-                      f"hierarchy levels bitwise the reference's"}
+            "sample": f"one CG solve of the same system on 1 core ({it} iterations, one oracle V-cycle each: "
+                      f"lexicographic Gauss-Seidel on the GPU-built levels, bitwise the reference's, and an "
+                      f"explicit inverse of the {A[-1].shape[0]}-row coarsest level)"}
 
 
 def main():

@@ -757,6 +757,16 @@ int orc_amg_from_levels(int n_level, const orc_csr *A, const orc_csr *P, int mos
   return 0;
 }
 
+int orc_amg_set_coarse_inverse(orc_amg *h, const double *inv) {
+  const int64_t n = h->n_coarse;
+  free(h->coarse_inv);
+  h->coarse_inv = (double *)malloc(sizeof(double) * (n * n ? n * n : 1));
+  if (!h->coarse_inv) return -1;
+  memcpy(h->coarse_inv, inv, sizeof(double) * n * n);
+  h->most_project_full = 1;
+  return 0;
+}
+
 int orc_lazy_project(const orc_csr *M, orc_csr *P, orc_csr *Pt) {
   const int64_t m = M->m;
   const int64_t *rs = M->rowptr, *cn = M->cols;

@@ -76,6 +76,10 @@ int orc_amg_setup(const orc_csr *a, int smooth_step, int64_t max_coarse, double 
  * hierarchy that was built (and checked equal to the reference's) elsewhere. */
 int orc_amg_from_levels(int n_level, const orc_csr *A, const orc_csr *P, int most_project_full,
                         int smooth_step, orc_amg *out);
+/* Replaces the coarsest inverse of a hierarchy with a given row-major
+ * n_coarse x n_coarse array (copied), for coarsest levels too large for the
+ * single-threaded inverse above to be practical. */
+int orc_amg_set_coarse_inverse(orc_amg *h, const double *inv);
 void orc_amg_free(orc_amg *h);
 /* Project() alone: C/F split and projection P for one level.
  * cf_out[i] = -1 for C-points, 1 for F-points (may be NULL). */

@@ -56,6 +56,7 @@ def lib():
         _lib.orc_amg_free.argtypes = [C.POINTER(_AMG)]
         _lib.orc_amg_from_levels.argtypes = [C.c_int, C.POINTER(_CSR), C.POINTER(_CSR), C.c_int, C.c_int,
                                              C.POINTER(_AMG)]
+        _lib.orc_amg_set_coarse_inverse.argtypes = [C.POINTER(_AMG), _f64p]
         _lib.orc_project.argtypes = [C.POINTER(_CSR), C.c_double, C.POINTER(_CSR), _i32p]
         _lib.orc_rap.argtypes = [C.POINTER(_CSR), C.POINTER(_CSR), C.POINTER(_CSR)]
         _lib.orc_amg_vcycles.argtypes = [C.POINTER(_AMG), _f64p, _f64p, C.c_int]
@@ -189,17 +190,24 @@ class AMG:
             raise RuntimeError("lazy re-setup failed")
 
     @classmethod
-    def from_levels(cls, A_levels, P_levels, most_project_full=True, smooth_step=3):
-        """A hierarchy built elsewhere: A_levels[0..L], P_levels[0..L-1] (CSR)."""
+    def from_levels(cls, A_levels, P_levels, most_project_full=True, smooth_step=3, coarse_inv=None):
+        """A hierarchy built elsewhere: A_levels[0..L], P_levels[0..L-1] (CSR).
+        coarse_inv (row-major, n_L x n_L) replaces the oracle's own inverse of
+        the coarsest level, for coarsest levels too large for it."""
         self = cls.__new__(cls)
         self._A = A_levels[0]
         L = len(P_levels)
         As = (_CSR * (L + 1))(*[a._c() for a in A_levels])
         Ps = (_CSR * max(L, 1))(*[p._c() for p in P_levels]) if L else (_CSR * 1)()
         self._h = _AMG()
-        rc = lib().orc_amg_from_levels(L, As, Ps, int(most_project_full), smooth_step, C.byref(self._h))
+        full = int(most_project_full) if coarse_inv is None else 0
+        rc = lib().orc_amg_from_levels(L, As, Ps, full, smooth_step, C.byref(self._h))
         if rc != 0:
             raise RuntimeError("singular coarsest matrix")
+        if coarse_inv is not None:
+            inv = np.ascontiguousarray(coarse_inv, dtype=np.float64)
+            if lib().orc_amg_set_coarse_inverse(C.byref(self._h), _ptr(inv, _f64p)) != 0:
+                raise RuntimeError("coarse inverse")
         return self
 
     def __del__(self):

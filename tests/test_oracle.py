@@ -70,3 +70,23 @@ def test_lazy_hierarchy_bitwise(name):
         assert np.array_equal(amg.level(l + 1).vals, ref.vals)
     x2 = amg.vcycles(np.zeros_like(g["rhs"]), g["rhs"], 3)
     assert np.allclose(x2, g["x_lazy2"], rtol=1e-11, atol=1e-13 * np.abs(g["x_lazy2"]).max())
+
+
+def test_from_levels_with_given_coarse_inverse():
+    """A hierarchy rebuilt from its levels, truncated above the coarsest level
+    and given that level's inverse from LAPACK, runs the same CG as the
+    oracle's own hierarchy truncated there (used for the timed CPU sample)."""
+    g = load_golden("tri_p1_16_coef")
+    S = golden_csr(g, "system")
+    amg = O.AMG(S)
+    L = min(2, amg.n_level)
+    A = [amg.level(l) for l in range(L + 1)]
+    P = [amg.projection(l) for l in range(L)]
+    own = O.AMG.from_levels(A, P)
+    inv = np.linalg.inv(A[-1].to_scipy().toarray())
+    given = O.AMG.from_levels(A, P, coarse_inv=inv)
+    b = g["rhs"]
+    x1, it1, _ = own.pcg(b, 1e-10)
+    x2, it2, _ = given.pcg(b, 1e-10)
+    assert it1 == it2
+    assert np.abs(x1 - x2).max() <= 1e-10 * np.abs(x1).max()
