@@ -15,7 +15,10 @@
 // restriction and prolongation are gathers without atomics.  The V-cycle is
 // captured once into a CUDA graph and replayed.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <numeric>
 
 #include "amg_internal.cuh"
@@ -26,10 +29,34 @@ using namespace afp;
 namespace afp {
 namespace {
 
+// A level of at most kDenseTailMax rows whose matrix is at least
+// kDenseTailDensity nonzero becomes the dense tail even above dense_tail
+// rows.  Measured on the 2D P2 512^2 hierarchy: the 12,554-row level is 12%
+// nonzero and the product that would coarsen it yields a 7,093-row level
+// that is 68% nonzero (the reference algorithm spends 411 s of 8-thread CPU
+// time on that one product); 3D P1 64^3 and 3D P2 tails are 9-14% nonzero.
+constexpr int64_t kDenseTailMax = 16384;
+constexpr double kDenseTailDensity = 0.05;
+
 struct DevCSR {
   int64_t m = 0, n = 0, nnz = 0;
   DevBuf<int> rp, ci;
   DevBuf<double> va;
+};
+
+// Setup trace: with AFP_SETUP_TRACE set, each setup step prints its wall
+// time (after a stream sync) to stderr.
+struct SetupTrace {
+  bool on = std::getenv("AFP_SETUP_TRACE") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void mark(const afp_context* ctx, const char* what, int level, int64_t n, int64_t nnz) {
+    if (!on) return;
+    sync(ctx);
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "[afp setup] level %d (n %lld, nnz %lld) %s: %.3f s\n", level, (long long)n,
+                 (long long)nnz, what, std::chrono::duration<double>(now - t).count());
+    t = now;
+  }
 };
 
 void upload_host_csr(const afp_context* ctx, const HostCSR& H, DevCSR& D) {
@@ -255,6 +282,7 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
   afp_context* ctx = h->ctx;
   const int t = h->t;
   const bool mixed = h->opts.precision == AFP_PRECISION_MIXED;
+  SetupTrace tr;
   h->lv.resize(t + 1);
   std::vector<std::vector<int>> perm(t + 1), iperm(t + 1);
   for (int l = 0; l <= t; ++l) {
@@ -320,6 +348,7 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
     }
     (void)diperm;
   }
+  tr.mark(ctx, "colouring + level permutation", t, h->lv[t].n, 0);
   // projections in the permuted numbering
   for (int l = 0; l < t; ++l) {
     Level& L = h->lv[l];
@@ -368,6 +397,7 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
     }
     sync(ctx);
   }
+  tr.mark(ctx, "P / P^T permutation", t, h->lv[t].n, 0);
   // tail
   Level& T = h->lv[t];
   if (h->tail_dense) {
@@ -388,6 +418,7 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
     T.va32.alloc(ctx, T.nnz);
     convert<double, float>(ctx, T.nnz, T.va.get(), T.va32.get());
   }
+  tr.mark(ctx, "dense tail inverse", t, h->lv[t].n, 0);
   const int64_t n0 = h->lv[0].n;
   h->b.alloc(ctx, n0);
   h->x.alloc(ctx, n0);
@@ -412,6 +443,7 @@ void setup(afp_amg* h, afp_matrix* A, bool lazy) {
   h->pat0 = A->pat;
   const afp_amg_opts& o = h->opts;
   AFP_REQUIRE(A->pat->m == A->pat->n, AFP_ERR_INVALID, "matrix is not square");
+  SetupTrace tr;
   HostCSR H0;
   download_host_csr(ctx, A->pat->m, A->pat->n, A->pat->nnz, A->pat->rowptr.get(), A->pat->cols.get(), A->vals.get(),
                     H0);
@@ -422,12 +454,20 @@ void setup(afp_amg* h, afp_matrix* A, bool lazy) {
   h->most_full = true;
   int l = 0;
   while (m > (uint64_t)o.max_coarse || sparse_degree < o.min_density) {
-    if (o.dense_tail > 0 && l > 0 && m <= (uint64_t)o.dense_tail) break;  // the dense tail starts here
+    // the dense tail starts here: at most dense_tail rows, or a level already
+    // dense enough (coarse levels of 2D P2 / 3D hierarchies) that the next
+    // Galerkin product would cost far more than inverting this level
+    if (o.dense_tail > 0 && l > 0) {
+      const double density = (double)h->refA[l].nnz() / ((double)m * (double)m);
+      if (m <= (uint64_t)o.dense_tail || (m <= (uint64_t)kDenseTailMax && density >= kDenseTailDensity)) break;
+    }
     const HostCSR& M = h->refA[l];
     std::vector<int> cf;
     HostCSR P, Pt;
+    tr.mark(ctx, "previous level done", l, M.m, M.nnz());
     if (lazy) host_lazy_project(M, P, Pt);
     else host_project(M, o.alpha, cf, P, Pt);
+    tr.mark(ctx, "host C/F + P", l, P.m, P.nnz());
     DevCSR dP, dT;
     upload_host_csr(ctx, P, dP);
     upload_host_csr(ctx, Pt, dT);
@@ -438,6 +478,7 @@ void setup(afp_amg* h, afp_matrix* A, bool lazy) {
     DevBuf<double> cvals;
     galerkin_product(ctx, P.m, P.n, dP.rp.get(), dP.ci.get(), dP.va.get(), arp, aci, ava, dT.rp.get(), dT.ci.get(),
                      dT.va.get(), cpat, cvals);
+    tr.mark(ctx, "GPU Galerkin product", l + 1, cpat.m, cpat.nnz);
     HostCSR C;
     download_host_csr(ctx, cpat.m, cpat.n, cpat.nnz, cpat.rowptr.get(), cpat.cols.get(), cvals.get(), C);
     m = (uint64_t)C.m;
@@ -463,7 +504,9 @@ void setup(afp_amg* h, afp_matrix* A, bool lazy) {
   h->n_project = l;
   h->t = l;
   h->tail_dense = h->most_full;
+  tr.mark(ctx, "hierarchy done", l, (int64_t)m, 0);
   build_solve_layout(h, refDev, A);
+  tr.mark(ctx, "solve layout (colouring, permutation, tail inverse)", h->t, h->lv[h->t].n, 0);
 }
 
 // AMGSolver::lazyReinit on an initialised solver (src/AMGSolver.cpp:505-545):

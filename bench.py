@@ -397,7 +397,11 @@ def run_stream(args):
             srv.reset_stats()
             s0 = time.perf_counter()
             tickets = [srv.submit(wl) for wl in wls]
-            res = [srv.wait(t)[1] for t in tickets]
+            res = []
+            for i, t in enumerate(tickets):
+                res.append(srv.wait(t)[1])
+                print(f"[bench] stream {name}: request {i + 1}/{len(tickets)} done "
+                      f"({res[-1]['latency_seconds']:.2f} s, n_dof {int(wls[i].space.n_dof)})", file=sys.stderr, flush=True)
             wall = time.perf_counter() - s0
             st = srv.stats()
             phase(f"stream: {name} server run")

@@ -144,9 +144,12 @@ typedef struct afp_amg_opts {
   double min_density;   /* n_most_project_sparse_degree (default 0.382)         */
   double alpha;         /* strong-connection threshold (default 0.25)           */
   int precision;        /* afp_precision of the V-cycle (default FP64)          */
-  int dense_tail;       /* levels with at most this many rows are solved with a
-                           dense inverse instead of smoothed (default 8192;
-                           0 keeps the reference depth)                         */
+  int dense_tail;       /* coarsening stops at the first coarse level with at
+                           most this many rows (default 8192, max 16384), or
+                           with at most 16384 rows and at least 5% of its
+                           entries nonzero; that level is solved with a dense
+                           inverse instead of smoothed (0 keeps the
+                           reference's full depth)                              */
   int max_colors;       /* colour classes of the smoother before rows fall into
                            an l1-Jacobi overflow class (default 32)             */
   int symmetric;        /* post-smoothing visits colours in reverse order so the
