@@ -766,7 +766,7 @@ void afp_amg_default_opts(afp_amg_opts* o) {
   o->dense_tail = 8192;
   o->max_colors = 32;
   o->symmetric = 1;
-  o->coarse_colors = 8;
+  o->coarse_colors = 4;
   o->interp_bf16 = 0;
   o->fused_vcycle = 0;
 }

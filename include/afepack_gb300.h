@@ -154,9 +154,13 @@ typedef struct afp_amg_opts {
                            an l1-Jacobi overflow class (default 32)             */
   int symmetric;        /* post-smoothing visits colours in reverse order so the
                            V-cycle is a symmetric preconditioner (default 1)    */
-  int coarse_colors;    /* colour-class cap on levels >= 1 (default 8; 0 = use
-                           max_colors); their long rows would otherwise need
-                           dozens of sequential classes                         */
+  int coarse_colors;    /* colour-class cap on levels >= 1 (default 4; 0 = use
+                           max_colors): their long rows would otherwise need
+                           dozens of sequential classes, one launch each; the
+                           rows beyond the cap form one l1-Jacobi class.  On
+                           the 3D P1 64^3 hierarchy caps of 8, 4 and 2 give
+                           21, 21 and 22 PCG iterations (CPU restatement of
+                           the V-cycle)                                         */
   int interp_bf16;      /* mixed precision only: keep P and P^T in BF16 (1) or
                            in FP32 (0, default: BF16 interpolation weights cost
                            the 3D P1 solve about 1.5x the PCG iterations)       */
