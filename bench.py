@@ -117,6 +117,63 @@ def phase(name):
     _CLOCK[0] = now
 
 
+def world_size():
+    return int(os.environ.get("WORLD_SIZE", "1"))
+
+
+def local_device():
+    return int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def dist_init():
+    """N > 1 (torchrun): one rank per GPU, each an independent replica of the
+    whole workload (the solve path does not shard); NCCL on GPUs, gloo else."""
+    import torch
+    import torch.distributed as dist
+    if world_size() > 1 and not dist.is_initialized():
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local_device())
+        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
+
+
+def barrier():
+    if world_size() > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def combine_replicas(line):
+    """Whole-job line for N replicas (called on every rank; rank 0's return
+    value is printed): every rank processed `steps` solves, so value = N solves
+    per step over the slowest rank's time per step (max over ranks), and the
+    same for the end-to-end figure; latencies are the slowest rank's."""
+    n = world_size()
+    if n == 1:
+        return line
+    import torch.distributed as dist
+    lines = [None] * n
+    dist.all_gather_object(lines, line)
+    out = dict(lines[0])
+    out["n_gpus"] = n
+    out["per_rank_value"] = [l["value"] for l in lines]
+    if any(l.get("ms_per_step") is None for l in lines):  # served stream: throughputs add up
+        out["value"] = round(sum(l["value"] for l in lines), 3)
+        return out
+    worst = max(lines, key=lambda l: l["ms_per_step"])
+    out["ms_per_step"] = worst["ms_per_step"]
+    out["value"] = round(n * 1e3 / worst["ms_per_step"], 3)
+    for key in ("p50_ms", "p99_ms"):
+        if key in worst:
+            out[key] = worst[key]
+    if isinstance(out.get("e2e"), dict):
+        e2e = dict(out["e2e"])
+        e2e["value"] = round(n * min(l["e2e"]["value"] for l in lines), 3)
+        out["e2e"] = e2e
+    out["cpu_baseline"] = None  # the CPU sample is taken at N = 1 only
+    out["config"] = dict(out["config"], parallelism=f"replicas only ({n} independent replicas, one per GPU)")
+    return out
+
+
 def profiled_traffic(workload):
     """DRAM bytes (read + write) of one fused V-cycle launch from the committed
     ncu summary of this workload, or None when there is none."""
@@ -153,8 +210,8 @@ def run_ours(args):
 
     B.build()
     torch.cuda.init()
-    dev = torch.device("cuda:0")
-    ctx = Context(0)
+    dev = torch.device(f"cuda:{local_device()}")
+    ctx = Context(local_device())
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     wl = WORKLOADS[args.workload](W)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -213,6 +270,8 @@ def run_ours(args):
             clocks.start()
         # named range of the timed solves ("timed_fp64" / "timed_mixed"), so a
         # profiler's launch list can be limited to them (ncu --nvtx-include)
+        torch.cuda.synchronize()
+        barrier()
         torch.cuda.nvtx.range_push(f"timed_{name}")
         for _ in range(args.steps):
             with torch.cuda.stream(stream):
@@ -225,6 +284,7 @@ def run_ours(args):
             times.append(s0.elapsed_time(s1))
             iters.append(info["iterations"])
         torch.cuda.nvtx.range_pop()
+        barrier()
         if name == "mixed":
             clk = clocks.stop()
         err = float(torch.linalg.norm(x - x_ref) / torch.linalg.norm(x_ref))
@@ -294,7 +354,7 @@ def run_ours(args):
     phase("kernel timings")
     launches = ctx.launch_count()
     # CPU baseline (rank 0, N=1): the reference algorithm's solve on one core
-    cpu = cpu_baseline_sample(amg64, b.cpu().numpy().copy(), args.tol)
+    cpu = cpu_baseline_sample(amg64, b.cpu().numpy().copy(), args.tol) if world_size() == 1 else None
     phase("CPU sample")
     line = {
         "metric": METRIC, "value": round(results["mixed"]["solves_per_s"], 3), "unit": "solves/s",
@@ -326,8 +386,8 @@ def run_multi(args):
     from afepack_gb300.amg import FP64, MIXED, AMGSolver
     from afepack_gb300.fem import BoundaryConditionAdmin, Context, Space, assemble
     B.build()
-    dev = torch.device("cuda:0")
-    ctx = Context(0)
+    dev = torch.device(f"cuda:{local_device()}")
+    ctx = Context(local_device())
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     wl = W.poisson3d_p2_multi(args.multi_n, args.nrhs)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -562,7 +622,9 @@ def main():
         if rank == 0:
             print(json.dumps(run_reference(args)))
         return
+    dist_init()
     line = run_stream(args) if args.stream else run_multi(args) if args.multi else run_ours(args)
+    line = combine_replicas(line)
     if rank == 0:
         print(json.dumps(line))
 
