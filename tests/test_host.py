@@ -102,3 +102,15 @@ def test_errors_without_gpu_are_reported(native):
     h = C.c_void_p()
     st = native.afp_context_create(10_000, C.byref(h))
     assert st in (1, 3)
+
+
+def test_amg_default_options():
+    """Defaults of afp_amg_opts as set by afp_amg_default_opts (host only):
+    the reference's AMGSolver parameters plus the GB300-side choices."""
+    from afepack_gb300.amg import default_opts
+    o = default_opts()
+    assert (o.tolerance, o.smooth_step, o.max_coarse) == (1e-12, 3, 50)
+    assert (o.min_density, o.alpha) == (0.382, 0.25)
+    assert o.precision == 0 and o.symmetric == 1
+    assert (o.dense_tail, o.max_colors, o.coarse_colors) == (8192, 32, 4)
+    assert o.interp_bf16 == 0 and o.fused_vcycle == 0
