@@ -54,9 +54,11 @@ def parse():
     ap.add_argument("--stream-sample", type=int, default=48)
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--multi", action="store_true", help="batched multi-RHS workload (3D P2, 64 RHS)")
-    # 24: at 48^3 the reference's C/F coarsening of 3D P2 fills in (a 75,511-row
-    # level with 80M entries) and setup does not finish in minutes
-    ap.add_argument("--multi-n", type=int, default=24)
+    ap.add_argument("--multi-n", type=int, default=48)
+    # lazy: the reference's lazyProject hierarchy (AMGPreconditioner's); the
+    # classical C/F hierarchy of 3D P2 at 48^3 fills in (a 75,511-row level
+    # with 80M entries) and its setup does not finish in minutes
+    ap.add_argument("--multi-hierarchy", default="lazy", choices=["lazy", "classical"])
     ap.add_argument("--nrhs", type=int, default=64)
     ap.add_argument("--tol-multi", type=float, default=1e-10)
     return ap.parse_args()
@@ -379,9 +381,10 @@ def run_ours(args):
 
 
 def run_multi(args):
-    """3D Poisson P2 on an n^3 Kuhn cube (default 24^3, 117,649 DOFs), one
-    matrix and hierarchy, 64 right-hand sides: one batched multi-RHS CG (FP32
-    V-cycle, FP64 recurrences) per step, against sequential FP64 CG solves."""
+    """3D Poisson P2 on an n^3 Kuhn cube (default 48^3, 912,673 DOFs), one
+    matrix and hierarchy (by default the reference's lazyProject hierarchy),
+    64 right-hand sides: one batched multi-RHS CG (FP32 V-cycle, FP64
+    recurrences) per step, against sequential FP64 CG solves."""
     import torch
     from afepack_gb300 import build as B
     from afepack_gb300 import workloads as W
@@ -404,10 +407,17 @@ def run_multi(args):
     Bm[d != 0] = 0.0
     t1 = time.perf_counter()
     phase("multi: assembly and right-hand sides")
-    amg32 = AMGSolver(K, precision=MIXED)
+    def hierarchy(precision):
+        if args.multi_hierarchy == "classical":
+            return AMGSolver(K, precision=precision)
+        amg = AMGSolver(precision=precision)
+        amg.lazyReinit(K)
+        return amg
+
+    amg32 = hierarchy(MIXED)
     t2 = time.perf_counter()
     phase("multi: mixed setup")
-    amg64 = AMGSolver(K, precision=FP64)
+    amg64 = hierarchy(FP64)
     phase("multi: fp64 setup")
     Bd = torch.from_numpy(np.ascontiguousarray(Bm)).to(dev)
 
@@ -449,7 +459,8 @@ def run_multi(args):
         "metric": METRIC, "value": round(value, 3), "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(float(t.mean()), 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 V-cycle + fp64 CG", "data": "synthetic (seeded)",
-        "config": {"workload": f"poisson3d_p2_{args.multi_n}_x{args.nrhs}", "n_dof": int(wl.space.n_dof),
+        "config": {"workload": f"poisson3d_p2_{args.multi_n}_x{args.nrhs}", "hierarchy": args.multi_hierarchy,
+                   "n_dof": int(wl.space.n_dof),
                    "nnz": int(K.n_nonzero_elements()), "nrhs": args.nrhs, "tol": args.tol_multi,
                    "l2": "flushed before every step (512 MB write)"},
         "rel_err_vs_fp64": err, "pcg_iterations_max": int(max(i["iterations"] for i in infos)),
