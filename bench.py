@@ -295,7 +295,8 @@ def run_ours(args):
         t = np.array(times)
         results[name] = {"solves_per_s": 1e3 * len(t) / t.sum(), "ms_mean": float(t.mean()),
                          "p50_ms": float(np.percentile(t, 50)), "p99_ms": float(np.percentile(t, 99)),
-                         "pcg_iterations": int(np.median(iters)), "rel_err_vs_fp64": err}
+                         "pcg_iterations": int(np.median(iters)),
+        "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 1), "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 1), "rel_err_vs_fp64": err}
 
     phase("timed solves")
     # ---- end to end through the C ABI with host buffers (H2D of b, D2H of x inside)
@@ -572,7 +573,7 @@ def run_reference(args):
         pipes.append(a)
         procs.append(p)
     os.environ["OMP_NUM_THREADS"] = "1"
-    walls, iters = [], []
+    walls, iters, lat = [], [], []
     for i in range(args.warmup + args.steps):
         s0 = time.perf_counter()
         for a in pipes:
@@ -582,6 +583,7 @@ def run_reference(args):
         if i >= args.warmup:
             walls.append(wall)
             iters.append(res[0][1])
+            lat.extend(r[0] for r in res)  # each worker's own solve time
     for p in procs:
         p.join()
     walls = np.array(walls)
@@ -595,6 +597,7 @@ def run_reference(args):
                    "levels": [list(map(int, (amg.level(l).shape[0], amg.level(l).nnz))) for l in range(amg.n_level + 1)],
                    "parallelism": f"{cores} single-threaded processes, one solve each per step"},
         "pcg_iterations": int(np.median(iters)),
+        "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 1), "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 1),
         "setup": {"assembly_dirichlet_s": round(t1 - t0, 2), "amg_reinit_s": round(t2 - t1, 2),
                   "amg_reinit_threads": cores},
         "cpu_baseline": {"value": round(value, 4), "unit": "solves/s", "cores": cores, "kind": "port",
