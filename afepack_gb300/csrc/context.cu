@@ -181,6 +181,7 @@ afp_status afp_context_create(int device, afp_context** out) {
     AFP_CUDA(cudaMalloc(&ctx->d_retire, 16 * sizeof(unsigned)));
     AFP_CUDA(cudaMemset(ctx->d_retire, 0, 16 * sizeof(unsigned)));
     AFP_CUDA(cudaMallocHost(&ctx->h_scalars, 64 * sizeof(double)));
+    noalloc_reserve(device);
     *out = ctx.release();
   });
 }

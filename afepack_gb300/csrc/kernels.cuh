@@ -17,6 +17,10 @@ void galerkin_product(const afp_context* ctx, int64_t n_c, int64_t n_f, const in
                       const int* pt_rowptr, const int* pt_cols, const double* pt_vals, Pattern& out_pat,
                       DevBuf<double>& out_vals);
 
+// Reserves afp_matrix_vmult_noalloc's static staging array on `device` (the
+// current device); called once per context creation (noalloc.cu).
+void noalloc_reserve(int device);
+
 // Host CSR (AFEPack layout) used by the coarsening.
 struct HostCSR {
   int64_t m = 0, n = 0;

@@ -6,9 +6,16 @@
 // arena up front, a process running under a hard device-memory cap, or a
 // time-step loop that must not let the allocator's pool grow (or stall on
 // it) inside the step.  This entry point stages x and y in one fixed array
-// of static device storage instead, which exists from the moment the library
-// is loaded on a GPU until the process exits (32 MiB on every GPU that loads
-// the library, whether or not this function is ever called).
+// of static device storage instead (32 MiB per GPU).
+//
+// When the array is reserved: the library is built without relocatable
+// device code, so this file is its own module, and CUDA loads modules lazily
+// by default -- the array would otherwise appear on a GPU only when the
+// module is first touched.  afp_context_create therefore looks the array up
+// on its device (noalloc_reserve below), which loads the module and reserves
+// the 32 MiB then; a caller that creates its context before handing the rest
+// of the device to its own arena never sees the array appear later.  The
+// array stays until the process exits.
 //
 // Limits and rules for the caller:
 //  * matrices with more than AFP_NOALLOC_MAX_ENTRIES (2^21) rows or columns
@@ -19,9 +26,10 @@
 //  * nothing in the array has to start at zero: x is copied over the first
 //    half in full and every row of y is written by the product, so the
 //    contents a previous call left behind are never read;
-//  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress, with that device current); make that first call
-//    before any stream capture begins on the calling thread.
+//  * the array's device address is looked up once per device ordinal (with
+//    that device current) and kept for the life of the process; this
+//    assumes the device's primary context lives as long, so do not call
+//    cudaDeviceReset on a device this library has used.
 #include <mutex>
 
 #include "common.cuh"
@@ -56,6 +64,13 @@ double* stage_on(int device) {
 }
 
 }  // namespace
+
+namespace afp {
+// Called by afp_context_create with `device` current: loads this module on
+// the device and records the array's address, so the 32 MiB are reserved
+// when the context is made, not inside a later afp_matrix_vmult_noalloc.
+void noalloc_reserve(int device) { (void)stage_on(device); }
+}  // namespace afp
 
 extern "C" afp_status afp_matrix_vmult_noalloc(afp_matrix* a, const double* x, double* y) {
   using namespace afp;

@@ -113,12 +113,14 @@ afp_status afp_matrix_vmult(afp_matrix *a, const double *x, double *y);
  * device when they call it (device memory already reserved by their own
  * arena, a hard device-memory cap, or a time-step loop whose allocator must
  * not grow).  x and y are staged in a fixed static device array of
- * 2 x AFP_NOALLOC_MAX_ENTRIES doubles (32 MiB, held by every GPU that loads
- * the library), so matrices with more rows or columns than that are refused
- * with AFP_ERR_UNSUPPORTED.  All calls share the array: calls whose GPU work
- * overlaps race.  Nothing in it needs to start at zero.  The first call on a
- * device looks up the array's device address; make it before any stream
- * capture. */
+ * 2 x AFP_NOALLOC_MAX_ENTRIES doubles (32 MiB), so matrices with more rows or
+ * columns than that are refused with AFP_ERR_UNSUPPORTED.  The array is
+ * reserved on a GPU by the first afp_context_create for that GPU (create the
+ * context before an arena takes the rest of the device) and kept until the
+ * process exits; its device address is looked up there too, once per device
+ * ordinal, which assumes the device's primary context is never reset
+ * (cudaDeviceReset) while the library is in use.  All calls share the array:
+ * calls whose GPU work overlaps race.  Nothing in it needs to start at zero. */
 #define AFP_NOALLOC_MAX_ENTRIES (1 << 21)
 afp_status afp_matrix_vmult_noalloc(afp_matrix *a, const double *x, double *y);
 afp_status afp_matrix_destroy(afp_matrix *a);

@@ -62,6 +62,63 @@ def test_noalloc_vmult_device_pointers(native, ctx):
     assert np.allclose(y.cpu().numpy(), np.arange(n) * d, rtol=1e-15)
 
 
+def _cudart():
+    for name in ("libcudart.so.13", "libcudart.so"):
+        try:
+            return C.CDLL(name)
+        except OSError:
+            continue
+    for d in ("/usr/local/cuda/lib64", "/usr/local/cuda/targets/sbsa-linux/lib",
+              "/usr/local/cuda/targets/x86_64-linux/lib"):
+        try:
+            return C.CDLL(f"{d}/libcudart.so")
+        except OSError:
+            continue
+    pytest.skip("no shared CUDA runtime to read the memory pool with")
+
+
+USED_MEM_HIGH, USED_MEM_CURRENT = 8, 7  # cudaMemPoolAttrUsedMemHigh / UsedMemCurrent
+
+
+def _pool_high_after(rt, pool, fn):
+    """Peak bytes in use from the device's default stream-ordered pool while fn
+    runs, above what was in use before (the pool serves cudaMallocAsync, the
+    library's device allocator)."""
+    import torch
+    torch.cuda.synchronize()
+    zero = C.c_uint64(0)
+    assert rt.cudaMemPoolSetAttribute(pool, USED_MEM_HIGH, C.byref(zero)) == 0
+    cur0, high = C.c_uint64(0), C.c_uint64(0)
+    assert rt.cudaMemPoolGetAttribute(pool, USED_MEM_CURRENT, C.byref(cur0)) == 0
+    fn()
+    torch.cuda.synchronize()
+    assert rt.cudaMemPoolGetAttribute(pool, USED_MEM_HIGH, C.byref(high)) == 0
+    return high.value - cur0.value
+
+
+def test_noalloc_vmult_allocates_nothing(native, ctx):
+    """The promise itself: after the context exists, calls neither take bytes
+    from the device's stream-ordered pool (which the ordinary vmult does, the
+    control below) nor change the device's free memory."""
+    import torch
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.fem import Space, assemble
+    wl = W.poisson2d_p1(64)
+    K, _ = assemble(Space(ctx, wl.space), wl.acc_stiff, wl.acc_mass)
+    x = np.random.default_rng(5).standard_normal(K.n())
+    y = np.zeros(K.m())
+    rt = _cudart()
+    pool = C.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(C.byref(pool), 0) == 0
+    assert _pool_high_after(rt, pool, lambda: _vmult(native, "afp_matrix_vmult", K, x)) > 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    grew = _pool_high_after(rt, pool, lambda: [_call(native, "afp_matrix_vmult_noalloc", K, x, y) for _ in range(3)])
+    free1, _ = torch.cuda.mem_get_info()
+    assert grew == 0
+    assert free1 == free0
+
+
 def test_noalloc_vmult_refuses_matrices_above_the_limit(native, ctx):
     from afepack_gb300.fem import SparseMatrix
     n = LIMIT + 1
