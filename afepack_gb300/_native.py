@@ -20,6 +20,10 @@ c_void_pp = C.POINTER(C.c_void_p)
 
 AFP_PRECISION_FP64 = 0
 AFP_PRECISION_MIXED = 1
+AFP_ERR_INVALID = 1
+AFP_ERR_NOT_CONVERGED = 5
+AFP_ERR_BREAKDOWN = 6
+AFP_ERR_TIMEOUT = 8
 
 
 class AFPError(RuntimeError):

@@ -141,7 +141,9 @@ class AMGSolver:
         if not hasattr(b, "data_ptr"):
             b = np.ascontiguousarray(b, dtype=np.float64)
         info = N.SolveInfo()
-        N.call("afp_pcg_solve", self.handle, N.ptr(x), N.ptr(b), tol, maxit, C.byref(info))
+        st = N.lib().afp_pcg_solve(self.handle, N.ptr(x), N.ptr(b), tol, maxit, C.byref(info))
+        if st != N.AFP_ERR_NOT_CONVERGED:  # the iteration limit is reported in info, as the reference prints it
+            N.check(st, "afp_pcg_solve")
         return x, info.as_dict()
 
     def pcg_multi(self, B, tol: float = 1e-8, maxit: int = 500, X=None):
@@ -156,7 +158,9 @@ class AMGSolver:
         if not hasattr(B, "data_ptr"):
             B = np.ascontiguousarray(B, dtype=np.float64)
         infos = (N.SolveInfo * nrhs)()
-        N.call("afp_pcg_solve_multi", self.handle, N.ptr(X), N.ptr(B), nrhs, tol, maxit, infos)
+        st = N.lib().afp_pcg_solve_multi(self.handle, N.ptr(X), N.ptr(B), nrhs, tol, maxit, infos)
+        if st != N.AFP_ERR_NOT_CONVERGED:
+            N.check(st, "afp_pcg_solve_multi")
         return X, [i.as_dict() for i in infos]
 
 

@@ -748,6 +748,9 @@ void pcg(afp_amg* h, double* x_user, const double* b_user, double tol, int maxit
     info->final_residual = rel;
     info->seconds = ms * 1e-3;
   }
+  if (!conv)
+    fail(AFP_ERR_NOT_CONVERGED, "CG reached its iteration limit (" + std::to_string(maxit) +
+                                    ") above the tolerance; x holds the last iterate");
 }
 
 }  // namespace
@@ -1008,8 +1011,10 @@ afp_status afp_pcg_solve_multi(afp_amg* h, double* X, const double* B, int nrhs,
     afp_context* ctx = h->ctx;
     bind(ctx);
     const int64_t n = h->lv[0].n;
+    bool all = true;
     if (nrhs <= 64) {
-      pcg_multi(h, X, B, nrhs, tol, maxit, info);
+      all = pcg_multi(h, X, B, nrhs, tol, maxit, info);
+      if (!all) fail(AFP_ERR_NOT_CONVERGED, "a column reached the CG iteration limit above the tolerance");
       return;
     }
     // wider blocks: batches of 64 columns through contiguous staging blocks
@@ -1020,11 +1025,12 @@ afp_status afp_pcg_solve_multi(afp_amg* h, double* X, const double* B, int nrhs,
                                  cudaMemcpyDefault, ctx->stream));
       AFP_CUDA(cudaMemcpy2DAsync(bX.get(), kc * sizeof(double), X + c0, nrhs * sizeof(double), kc * sizeof(double), n,
                                  cudaMemcpyDefault, ctx->stream));
-      pcg_multi(h, bX.get(), bB.get(), kc, tol, maxit, info ? info + c0 : nullptr);
+      all = pcg_multi(h, bX.get(), bB.get(), kc, tol, maxit, info ? info + c0 : nullptr) && all;
       AFP_CUDA(cudaMemcpy2DAsync(X + c0, nrhs * sizeof(double), bX.get(), kc * sizeof(double), kc * sizeof(double), n,
                                  cudaMemcpyDefault, ctx->stream));
     }
     sync(ctx);
+    if (!all) fail(AFP_ERR_NOT_CONVERGED, "a column reached the CG iteration limit above the tolerance");
   });
 }
 

@@ -157,8 +157,9 @@ struct afp_amg {
 };
 
 namespace afp {
-// Batched CG over nrhs columns (mrhs.cu).
-void pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, double tol, int maxit,
+// Batched CG over nrhs columns (mrhs.cu); false when a column stopped at
+// the iteration limit above the tolerance.
+bool pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, double tol, int maxit,
                afp_solve_info* info);
 // Fused FP32 V-cycle (vcycle_fused.cu): plan from the solve layout (leaves
 // h->fused empty when it does not apply), launch, and the barrier-timeout flag.

@@ -70,7 +70,14 @@ def emit(name, dim, rules, max_acc, out):
 
 
 def main():
-    tdir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/include/AFEPack/template"
+    if len(sys.argv) > 1:
+        tdir = sys.argv[1]
+    else:
+        sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "oracle"))
+        import refpath
+        tdir = refpath.template_dir()
+        if tdir is None:
+            sys.exit("AFEPack sources not found: set AFEPACK_SOURCE or pass the template directory")
     tri = parse(os.path.join(tdir, "triangle", "triangle.tmp_geo"), 2)
     tet = parse(os.path.join(tdir, "tetrahedron", "tetrahedron.tmp_geo"), 3)
     out = ["// Generated by gen_quadrature.py from AFEPack's triangle.tmp_geo and",

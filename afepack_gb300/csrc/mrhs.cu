@@ -567,7 +567,7 @@ void precondition_m(afp_amg* h) {
 }  // namespace
 
 // Batched CG over up to 64 columns (callers chunk wider blocks).
-void pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, double tol, int maxit,
+bool pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, double tol, int maxit,
                afp_solve_info* info) {
   afp_context* ctx = h->ctx;
   const int k = nrhs;
@@ -682,6 +682,9 @@ void pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, doubl
       info[c].final_residual = rel[c];
       info[c].seconds = ms * 1e-3;
     }
+  for (int c = 0; c < k; ++c)
+    if (!(rel[c] <= tol)) return false;
+  return true;
 }
 
 }  // namespace afp

@@ -178,19 +178,6 @@ def combine_replicas(line):
     return out
 
 
-def profiled_traffic(workload):
-    """DRAM bytes (read + write) of one fused V-cycle launch from the committed
-    ncu summary of this workload, or None when there is none."""
-    path = os.path.join(ROOT, "profiles", f"vcycle_fused_{workload}.md")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return int(float(line.split(":", 1)[1]))
-    except OSError:
-        pass
-    return None
-
-
 def profiled_ratio(workload):
     """DRAM bytes over algorithmic bytes of a colour-class launch, from the
     committed ncu summary of this workload (None without one); the sweep's
@@ -336,20 +323,14 @@ def run_ours(args):
         per_unit = (ctx.launch_count() - c0) / (reps + 1)  # the timer runs one warm-up unit first
         kernels[label] = {"ms": round(ms, 5), "bytes": int(nbytes), "GBps": round(nbytes / ms / 1e6, 1),
                           "frac": round(nbytes / ms / 1e6 / hbm, 4), "launches": round(per_unit, 2)}
-    fused = kernels["vcycle_mixed"]["launches"] <= 1.5
-    if fused:
-        dom = kernels["vcycle_mixed"]
-        name = "k_vcycle_fused: one FP32 V-cycle (all levels, dense tail) in one cooperative launch"
-        traffic = profiled_traffic(args.workload)
-    else:
-        # the Gauss-Seidel sweep of the level that takes longest (levels 1-2
-        # of the 3D hierarchies: the largest share of the ncu launch list)
-        lev = max(range(len(levels) - 1), key=lambda l: kernels[f"gs_sweep_level{l}_mixed"]["ms"])
-        dom = kernels[f"gs_sweep_level{lev}_mixed"]
-        name = (f"k_gs_class<float> (+ k_jacobi_l1 overflow class): one Gauss-Seidel sweep of level {lev} "
-                f"({levels[lev][0]} rows, {dom['launches']:.0f} launches)")
-        ratio = profiled_ratio(args.workload)
-        traffic = int(ratio * dom["bytes"]) if ratio else None
+    # the Gauss-Seidel sweep of the level that takes longest (levels 1-2 of
+    # the 3D hierarchies: the largest share of the ncu launch list)
+    lev = max(range(len(levels) - 1), key=lambda l: kernels[f"gs_sweep_level{l}_mixed"]["ms"])
+    dom = kernels[f"gs_sweep_level{lev}_mixed"]
+    name = (f"k_gs_class<float> (+ k_jacobi_l1 overflow class): one Gauss-Seidel sweep of level {lev} "
+            f"({levels[lev][0]} rows, {dom['launches']:.0f} launches)")
+    ratio = profiled_ratio(args.workload)
+    traffic = int(ratio * dom["bytes"]) if ratio else None
     roof = {"bound": "hbm", "kernel": name, "achieved": dom["GBps"], "peak": hbm, "unit": "GB/s",
             "frac": dom["frac"], "traffic": traffic,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800 GB/s",
@@ -358,7 +339,8 @@ def run_ours(args):
     phase("kernel timings")
     launches = ctx.launch_count()
     # CPU baseline (rank 0, N=1): the reference algorithm's solve on one core
-    cpu = cpu_baseline_sample(amg64, b.cpu().numpy().copy(), args.tol) if world_size() == 1 else None
+    cpu = (cpu_baseline_sample(amg64, b.cpu().numpy().copy(), args.tol, results["fp64"]["pcg_iterations"])
+           if world_size() == 1 else None)
     phase("CPU sample")
     line = {
         "metric": METRIC, "value": round(results["mixed"]["solves_per_s"], 3), "unit": "solves/s",
@@ -605,14 +587,17 @@ def run_reference(args):
     }
 
 
-def cpu_baseline_sample(amg_gpu, b_host, tol):
-    """One single-threaded oracle CG solve (the reference's CG shape, one
-    reference V-cycle per iteration: lexicographic Gauss-Seidel, restriction,
+def cpu_baseline_sample(amg_gpu, b_host, tol, iterations, budget_s=20.0):
+    """Single-threaded oracle CG (the reference's CG shape, one reference
+    V-cycle per iteration: lexicographic Gauss-Seidel, restriction,
     prolongation) on the hierarchy the GPU built -- levels bitwise the
     reference's down to the dense tail -- with the reference's coarsest
     treatment, an explicit inverse, applied at that tail level (inverted here
     with LAPACK; the reference would keep coarsening it on the host for
-    minutes)."""
+    minutes).  Bounded by time: one iteration is timed first; when the whole
+    solve (`iterations`, the GPU FP64 solve's count) would take longer than
+    `budget_s`, as many iterations as fit are timed and the solve time is
+    extrapolated linearly from them."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
@@ -622,12 +607,19 @@ def cpu_baseline_sample(amg_gpu, b_host, tol):
     inv = np.linalg.inv(A[-1].to_scipy().toarray())
     amg = O.AMG.from_levels(A, P, coarse_inv=inv)
     t0 = time.perf_counter()
-    x, it, rel = amg.pcg(b_host, tol, 1000)
+    amg.pcg(b_host, 0.0, 1)
+    t1 = time.perf_counter() - t0
+    k = int(max(1, min(iterations, budget_s // max(t1, 1e-9))))
+    t0 = time.perf_counter()
+    x, it, rel = amg.pcg(b_host, tol if k >= iterations else 0.0, k)
     dt = time.perf_counter() - t0
-    return {"value": round(1.0 / dt, 4), "unit": "solves/s", "cores": 1, "kind": "port",
-            "sample": f"one CG solve of the same system on 1 core ({it} iterations, one oracle V-cycle each: "
-                      f"lexicographic Gauss-Seidel on the GPU-built levels, bitwise the reference's, and an "
-                      f"explicit inverse of the {A[-1].shape[0]}-row coarsest level)"}
+    solve_s = dt if k >= iterations else dt / it * iterations
+    how = (f"one whole CG solve ({it} iterations)" if k >= iterations else
+           f"{it} of {iterations} CG iterations timed ({dt:.1f} s), the solve extrapolated linearly")
+    return {"value": round(1.0 / solve_s, 4), "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": f"{how} of the same system on 1 core, one oracle V-cycle per iteration: lexicographic "
+                      f"Gauss-Seidel on the GPU-built levels, bitwise the reference's, and an explicit inverse "
+                      f"of the {A[-1].shape[0]}-row coarsest level"}
 
 
 def main():

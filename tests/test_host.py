@@ -49,8 +49,9 @@ def test_quadrature_tables():
         pts = np.array([[float(v) for v in row.split(",") if v.strip()] for row in re.findall(r"\{([^}]*)\}", body)])
         for a, b in zip(offs[:-1], offs[1:]):
             assert abs(pts[a:b, dim].sum() - 1.0) < 2e-7  # weights of each rule sum to one
-    tdir = "/root/reference/include/AFEPack/template"
-    if os.path.isdir(tdir):
+    import refpath
+    tdir = refpath.template_dir()
+    if tdir is not None:
         tri = G.parse(os.path.join(tdir, "triangle", "triangle.tmp_geo"), 2)
         assert len(tri[4]) == 6 and tri[4][0][0] == 0.445948490915965
 
