@@ -28,7 +28,7 @@ SOURCES = [
     ("solve.cu", []),
     ("amg.cu", []),
     ("mrhs.cu", []),
-    ("vcycle_fused.cu", []),
+    ("vcycle_stream.cu", []),
     ("noalloc.cu", []),
     ("coarsen_host.cpp", []),
     ("server.cpp", []),

@@ -161,7 +161,7 @@ void vcycle(afp_amg* h, X* x0, const X* r0, bool zero_init) {
   const X* rt = t == 0 ? r0 : lvr<X>(h, t);
   if (h->tail_dense) {
     if constexpr (std::is_same<X, double>::value) dense_gemv<double>(ctx, h->lv[t].n, h->tail_inv.get(), rt, xt);
-    else dense_gemv_df(ctx, h->lv[t].n, h->tail_hi.get(), h->tail_lo.get(), rt, xt);
+    else dense_gemv_df(ctx, h->lv[t].n, h->tail_ld, h->tail_hi.get(), h->tail_lo.get(), rt, xt);
   } else {
     diag_solve<X>(ctx, h->lv[t].A<X>(), rt, xt);
   }
@@ -175,16 +175,31 @@ void vcycle(afp_amg* h, X* x0, const X* r0, bool zero_init) {
   }
 }
 
-// Mixed-precision V-cycle: FP32 levels, P / P^T in BF16 or FP32 (opts.interp_bf16);
-// one cooperative kernel when the fused plan exists, else the launch chain.
+// Mixed-precision V-cycle as the launch chain: FP32 levels, P / P^T in BF16
+// or FP32 (opts.interp_bf16).
 void vcycle_mixed(afp_amg* h, float* x0, const float* r0) {
-  if (h->fused) fused_vcycle(h, x0, r0);
-  else if (h->opts.interp_bf16) vcycle<float, __nv_bfloat16>(h, x0, r0, true);
+  if (h->opts.interp_bf16) vcycle<float, __nv_bfloat16>(h, x0, r0, true);
   else vcycle<float, float>(h, x0, r0, true);
 }
 
-// Runs a graph build; if it fails while the fused V-cycle is in use (a graph
-// that cannot hold a cooperative kernel), drops the fused plan and retries
+// z = V(r) on the solver's level-0 buffers (FP64 in and out): the streamed
+// kernel when its plan exists (it converts r and z itself), else the chain.
+void vcycle_level0(afp_amg* h) {
+  afp_context* ctx = h->ctx;
+  const int64_t n = h->lv[0].n;
+  if (h->opts.precision != AFP_PRECISION_MIXED) {
+    vcycle<double, double>(h, h->z.get(), h->r.get(), true);
+  } else if (h->fused) {
+    fused_vcycle(h, h->r.get(), h->z.get());
+  } else {
+    convert<double, float>(ctx, n, h->r.get(), h->r32.get());
+    vcycle_mixed(h, h->z32.get(), h->r32.get());
+    convert<float, double>(ctx, n, h->z32.get(), h->z.get());
+  }
+}
+
+// Runs a graph build; if it fails while the streamed V-cycle is in use (a
+// graph that cannot hold a cooperative kernel), drops its plan and retries
 // with the launch chain.
 void drop_fused(afp_amg* h) {
   // graphs captured with the fused kernel refer to the plan's buffers
@@ -207,11 +222,11 @@ void with_chain_fallback(afp_amg* h, F&& build) {
 }
 
 void check_fused(afp_amg* h) {
-  if (fused_timed_out(h)) fail(AFP_ERR_TIMEOUT, "fused V-cycle: a grid barrier wait ran out");
+  if (fused_timed_out(h)) fail(AFP_ERR_TIMEOUT, "streamed V-cycle: a bounded wait ran out");
 }
 
 // Captures (once) and replays the preconditioner z = V(r) on the solver's
-// own level-0 buffers: FP64 on (r, z), mixed on (r32, z32).
+// own level-0 buffers (r, z).
 void precondition(afp_amg* h) {
   afp_context* ctx = h->ctx;
   const bool mixed = h->opts.precision == AFP_PRECISION_MIXED;
@@ -223,8 +238,7 @@ void precondition(afp_amg* h) {
       const int64_t before = ctx->launches.n;
       AFP_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
       try {
-        if (mixed) vcycle_mixed(h, h->z32.get(), h->r32.get());
-        else vcycle<double, double>(h, h->z.get(), h->r.get(), true);
+        vcycle_level0(h);
       } catch (...) {
         cudaStreamEndCapture(ctx->stream, &g);
         if (g) cudaGraphDestroy(g);
@@ -241,10 +255,8 @@ void precondition(afp_amg* h) {
       nodes = captured;
     });
   }
-  if (mixed) convert<double, float>(ctx, h->lv[0].n, h->r.get(), h->r32.get());
   AFP_CUDA(cudaGraphLaunch(exec, ctx->stream));
   ctx->launches.n += nodes;
-  if (mixed) convert<float, double>(ctx, h->lv[0].n, h->z32.get(), h->z.get());
 }
 
 __global__ void k_abs_residual_sum(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci,
@@ -336,15 +348,18 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
       L.va32.alloc(ctx, L.nnz);
       convert<double, float>(ctx, L.nnz, L.va.get(), L.va32.get());
     }
-    if (l > 0 || true) {
-      L.x.alloc(ctx, L.n);
-      L.r.alloc(ctx, L.n);
-      L.tmp.alloc(ctx, L.n);
-      if (mixed) {
-        L.x32.alloc(ctx, L.n);
-        L.r32.alloc(ctx, L.n);
-        L.tmp32.alloc(ctx, L.n);
-      }
+    L.x.alloc(ctx, L.n);
+    L.r.alloc(ctx, L.n);
+    L.tmp.alloc(ctx, L.n);
+    if (mixed) {
+      // four spare zeros: the streamed dense tail reads r in float4 runs up
+      // to the tail's padded row length
+      L.x32.alloc(ctx, L.n + 4);
+      L.r32.alloc(ctx, L.n + 4);
+      L.tmp32.alloc(ctx, L.n + 4);
+      L.x32.zero();
+      L.r32.zero();
+      L.tmp32.zero();
     }
     (void)diperm;
   }
@@ -407,9 +422,10 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
     if (mixed) {
       // FP32 pair with FP64-class accuracy: a plain FP32 inverse summed in
       // FP32 loses the coarse correction on ill-conditioned 3D tails
-      h->tail_hi.alloc(ctx, T.n * T.n);
-      h->tail_lo.alloc(ctx, T.n * T.n);
-      split_df(ctx, T.n * T.n, h->tail_inv.get(), h->tail_hi.get(), h->tail_lo.get());
+      h->tail_ld = (T.n + 3) / 4 * 4;
+      h->tail_hi.alloc(ctx, T.n * h->tail_ld);
+      h->tail_lo.alloc(ctx, T.n * h->tail_ld);
+      split_df(ctx, T.n, h->tail_ld, h->tail_inv.get(), h->tail_hi.get(), h->tail_lo.get());
       sync(ctx);
       h->tail_inv = DevBuf<double>();  // the FP64 V-cycle is not used at this precision
     }
@@ -432,8 +448,7 @@ void build_solve_layout(afp_amg* h, std::vector<DevCSR>& refDev, const afp_matri
     h->z32.alloc(ctx, n0);
   }
   sync(ctx);
-  static const bool no_fused = std::getenv("AFP_NO_FUSED") != nullptr;  // A/B timing of the launch chain
-  if (mixed && h->opts.fused_vcycle && !no_fused) fused_build(h);
+  if (mixed && h->opts.fused_vcycle) fused_build(h);
   else h->fused.reset();
 }
 
@@ -580,17 +595,7 @@ __global__ void k_copy_scalar(double* s, int from, int to) {
 }
 
 // z = M r on the solver's level-0 buffers, launched into the current capture
-void precondition_inline(afp_amg* h) {
-  afp_context* ctx = h->ctx;
-  const int64_t n = h->lv[0].n;
-  if (h->opts.precision == AFP_PRECISION_MIXED) {
-    convert<double, float>(ctx, n, h->r.get(), h->r32.get());
-    vcycle_mixed(h, h->z32.get(), h->r32.get());
-    convert<float, double>(ctx, n, h->z32.get(), h->z.get());
-  } else {
-    vcycle<double, double>(h, h->z.get(), h->r.get(), true);
-  }
-}
+void precondition_inline(afp_amg* h) { vcycle_level0(h); }
 
 void pcg_iteration_tail(afp_amg* h, double* s, cudaGraphConditionalHandle handle) {
   afp_context* ctx = h->ctx;
@@ -705,6 +710,7 @@ void pcg(afp_amg* h, double* x_user, const double* b_user, double tol, int maxit
     sync(ctx);
     it = lv[0];
     ctx->launches.n += h->loop_pre_nodes[pi] + (int64_t)(it - 1) * h->loop_body_nodes[pi];
+    check_fused(h);  // a V-cycle that gave up leaves z undefined: report that first
     rel = std::sqrt(rr) / bn;
     check_finite(rel, "residual");
     conv = rel <= tol;
@@ -720,6 +726,7 @@ void pcg(afp_amg* h, double* x_user, const double* b_user, double tol, int maxit
       copy(ctx, &rr, s + 2, sizeof(double));
       sync(ctx);
       rel = std::sqrt(rr) / bn;
+      check_fused(h);
       check_finite(rel, "residual");
       if (rel <= tol) {
         conv = true;
@@ -771,7 +778,9 @@ void afp_amg_default_opts(afp_amg_opts* o) {
   o->symmetric = 1;
   o->coarse_colors = 4;
   o->interp_bf16 = 0;
-  o->fused_vcycle = 0;
+  o->fused_vcycle = 1;
+  o->wait_limit_s = 2.0;
+  o->inject_barrier_stall = 0;
 }
 
 afp_status afp_amg_setup(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out) {
@@ -784,7 +793,8 @@ afp_status afp_amg_setup(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out)
     else afp_amg_default_opts(&h->opts);
     const afp_amg_opts& o = h->opts;
     AFP_REQUIRE(o.smooth_step >= 0 && o.max_coarse >= 1 && o.alpha >= 0 && o.max_colors >= 1 && o.dense_tail >= 0 &&
-                    (o.precision == AFP_PRECISION_FP64 || o.precision == AFP_PRECISION_MIXED),
+                    (o.precision == AFP_PRECISION_FP64 || o.precision == AFP_PRECISION_MIXED) &&
+                    o.wait_limit_s > 0 && o.wait_limit_s <= 60,
                 AFP_ERR_INVALID, "invalid AMG options");
     AFP_REQUIRE(o.dense_tail <= 16384, AFP_ERR_UNSUPPORTED, "dense_tail above 16384 rows");
     setup(h.get(), a, false);
@@ -920,6 +930,11 @@ afp_status afp_amg_time_kernel(afp_amg* h, int kind, int level, int reps, double
       std::vector<float> one(n, 1.0f);
       copy(ctx, level == 0 ? h->r32.get() : L.r32.get(), one.data(), sizeof(float) * n);
       fill_zero<float>(ctx, n, level == 0 ? h->z32.get() : L.x32.get());
+      if (level == 0) {  // the streamed V-cycle reads the FP64 r
+        std::vector<double> one64(n, 1.0);
+        copy(ctx, h->r.get(), one64.data(), sizeof(double) * n);
+        sync(ctx);
+      }
     } else {
       std::vector<double> one(n, 1.0);
       copy(ctx, level == 0 ? h->r.get() : L.r.get(), one.data(), sizeof(double) * n);
@@ -951,7 +966,8 @@ afp_status afp_amg_time_kernel(afp_amg* h, int kind, int level, int reps, double
           }
         }
       } else if (kind == 2) {
-        if (mixed) vcycle_mixed(h, h->z32.get(), h->r32.get());
+        if (mixed && h->fused) fused_vcycle(h, h->r.get(), h->z.get());
+        else if (mixed) vcycle_mixed(h, h->z32.get(), h->r32.get());
         else vcycle<double, double>(h, h->z.get(), h->r.get(), true);
       } else {
         spmv<double, double>(ctx, h->lv[0].A<double>(), h->p.get(), h->q.get(), false);
@@ -971,6 +987,7 @@ afp_status afp_amg_time_kernel(afp_amg* h, int kind, int level, int reps, double
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms = t / reps;
+    if (kind == 2) fused_print_trace(h);  // AFP_VCYCLE_TRACE: per-phase times of the last V-cycle
     const double mat = (double)L.nnz * (v + 4) + 4.0 * (n + 1);
     if (kind == 0) *bytes = mat + 3.0 * n * v;           // read r, x gathers once, write x
     else if (kind == 1) *bytes = mat + 3.0 * n * v;      // read x, r, write out

@@ -189,7 +189,7 @@ __global__ void k_dense_gemm(int64_t n, const X* __restrict__ M, const X* __rest
 // FP32 V-cycle tail: X = (hi + lo) R with a double-float pair per column
 // (the single-column kernel's accumulation, see df32.cuh)
 template <int KPL>
-__global__ void k_dense_gemm_df(int64_t n, const float* __restrict__ hi, const float* __restrict__ lo,
+__global__ void k_dense_gemm_df(int64_t n, int64_t ld, const float* __restrict__ hi, const float* __restrict__ lo,
                                 const float* __restrict__ r, float* __restrict__ x, int k) {
   const int lane = threadIdx.x & 31;
   for (int64_t row = warp_id(); row < n; row += n_warps()) {
@@ -197,7 +197,7 @@ __global__ void k_dense_gemm_df(int64_t n, const float* __restrict__ hi, const f
 #pragma unroll
     for (int q = 0; q < KPL; ++q) sh[q] = sl[q] = 0.f;
     for (int64_t j = 0; j < n; ++j) {
-      const float a = hi[row * n + j], b = lo[row * n + j];
+      const float a = hi[row * ld + j], b = lo[row * ld + j];
 #pragma unroll
       for (int q = 0; q < KPL; ++q) {
         const int c = lane + 32 * q;
@@ -463,7 +463,7 @@ void vcycle_m(afp_amg* h, MultiState& S) {
         k_dense_gemm<KPL, X><<<rows_grid(ctx, T.n), BLK, 0, ctx->stream>>>(T.n, h->tail_inv.get(), blk<X>(S, 1, t),
                                                                           blk<X>(S, 0, t), k);
       else
-        k_dense_gemm_df<KPL><<<rows_grid(ctx, T.n), BLK, 0, ctx->stream>>>(T.n, h->tail_hi.get(), h->tail_lo.get(),
+        k_dense_gemm_df<KPL><<<rows_grid(ctx, T.n), BLK, 0, ctx->stream>>>(T.n, h->tail_ld, h->tail_hi.get(), h->tail_lo.get(),
                                                                           blk<X>(S, 1, t), blk<X>(S, 0, t), k);
       check_launch(ctx, "mrhs dense tail");
     } else {

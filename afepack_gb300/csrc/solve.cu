@@ -197,27 +197,28 @@ __global__ void k_dense_gemv(int64_t n, const X* __restrict__ M, const X* __rest
   if (row < n && lane == 0) x[row] = (X)s;
 }
 
-__global__ void k_split_df(int64_t n, const double* __restrict__ in, float* __restrict__ hi,
+__global__ void k_split_df(int64_t n, int64_t ld, const double* __restrict__ in, float* __restrict__ hi,
                            float* __restrict__ lo) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double d = in[i];
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * ld) return;
+  const int64_t i = t / ld, j = t % ld;
+  const double d = j < n ? in[i * n + j] : 0.0;
   const float h = __double2float_rn(d);
-  hi[i] = h;
-  lo[i] = __double2float_rn(d - (double)h);
+  hi[t] = h;
+  lo[t] = __double2float_rn(d - (double)h);
 }
 
 // One warp per row; each lane walks the row with stride 32 (coalesced loads of
 // hi and lo), accumulating a double-float pair; the pairs are merged across
 // the warp with TwoSum.
-__global__ void k_dense_gemv_df(int64_t n, const float* __restrict__ hi, const float* __restrict__ lo,
+__global__ void k_dense_gemv_df(int64_t n, int64_t ld, const float* __restrict__ hi, const float* __restrict__ lo,
                                 const float* __restrict__ r, float* __restrict__ x) {
   pdl_wait();
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x & 31;
   if (row >= n) return;  // whole warps leave together
-  const float* h = hi + row * n;
-  const float* l = lo + row * n;
+  const float* h = hi + row * ld;
+  const float* l = lo + row * ld;
   float sh = 0.f, sl = 0.f;
   int64_t j = lane;
   for (; j + 96 < n; j += 128) {
@@ -563,15 +564,16 @@ void dense_gemv(const afp_context* ctx, int64_t n, const X* Ainv, const X* r, X*
   check_launch(ctx, "dense gemv");
 }
 
-void split_df(const afp_context* ctx, int64_t n2, const double* inv, float* hi, float* lo) {
-  if (n2 == 0) return;
-  k_split_df<<<grid_for(n2, BLK), BLK, 0, ctx->stream>>>(n2, inv, hi, lo);
+void split_df(const afp_context* ctx, int64_t n, int64_t ld, const double* inv, float* hi, float* lo) {
+  if (n == 0) return;
+  k_split_df<<<grid_for(n * ld, BLK), BLK, 0, ctx->stream>>>(n, ld, inv, hi, lo);
   check_launch(ctx, "double-float split");
 }
 
-void dense_gemv_df(const afp_context* ctx, int64_t n, const float* hi, const float* lo, const float* r, float* x) {
+void dense_gemv_df(const afp_context* ctx, int64_t n, int64_t ld, const float* hi, const float* lo, const float* r,
+                   float* x) {
   if (n == 0) return;
-  launch_pdl(ctx->stream, grid_for(n * 32, BLK), BLK, 0, k_dense_gemv_df, n, hi, lo, r, x);
+  launch_pdl(ctx->stream, grid_for(n * 32, BLK), BLK, 0, k_dense_gemv_df, n, ld, hi, lo, r, x);
   check_launch(ctx, "dense gemv (double-float)");
 }
 

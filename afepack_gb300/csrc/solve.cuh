@@ -42,12 +42,15 @@ void jacobi_l1_class(const afp_context* ctx, const CSRView<X>& A, int64_t r0, in
 template <class X>
 void dense_gemv(const afp_context* ctx, int64_t n, const X* Ainv, const X* r, X* x);
 
-// FP64 inverse -> FP32 pair (hi, lo) with hi + lo == inv to ~2^-48 (n2 entries).
-void split_df(const afp_context* ctx, int64_t n2, const double* inv, float* hi, float* lo);
+// FP64 n x n inverse -> FP32 pair (hi, lo) with hi + lo == inv to ~2^-48;
+// the pair's rows have stride ld >= n (a multiple of 4, so that every row
+// starts 16-byte aligned) and zeros in columns [n, ld).
+void split_df(const afp_context* ctx, int64_t n, int64_t ld, const double* inv, float* hi, float* lo);
 
 // x = (hi + lo) r in FP32 with double-float accumulation (the FP32 V-cycle's
-// dense coarsest solve; see df32.cuh).
-void dense_gemv_df(const afp_context* ctx, int64_t n, const float* hi, const float* lo, const float* r, float* x);
+// dense coarsest solve; see df32.cuh); rows of the pair have stride ld.
+void dense_gemv_df(const afp_context* ctx, int64_t n, int64_t ld, const float* hi, const float* lo, const float* r,
+                   float* x);
 
 // x_j = r_j / a_jj (coarsest level when it is not full).
 template <class X>

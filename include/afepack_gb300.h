@@ -166,15 +166,26 @@ typedef struct afp_amg_opts {
   int interp_bf16;      /* mixed precision only: keep P and P^T in BF16 (1) or
                            in FP32 (0, default: BF16 interpolation weights cost
                            the 3D P1 solve about 1.5x the PCG iterations)       */
-  int fused_vcycle;     /* mixed precision: run each V-cycle as one cooperative
-                           kernel with grid barriers instead of a chain of
-                           ~150-200 PDL launches (1), or as the chain (0,
-                           default: on GB300 a grid barrier measured ~4-5 us,
-                           more than a chained launch, so the chain is faster:
-                           1.03 ms vs 1.71 ms per 64^3 P1 V-cycle).  Both give
-                           the same iterates bit for bit.  Two such kernels
-                           running at once on one GPU compete for its SMs, so
-                           the server's concurrent workers never use it. */
+  int fused_vcycle;     /* mixed precision: run each V-cycle as one persistent
+                           kernel (1, default) instead of a chain of ~130 PDL
+                           launches (0).  The kernel keeps one CTA per SM and
+                           streams every CTA's share of the level operators
+                           through a ring of shared-memory slots with bulk
+                           async copies; colour classes wait only for the CTAs
+                           that own coupled rows, level changes for the whole
+                           grid.  It needs the whole GPU, so the server's
+                           concurrent workers use the chain.  Where the plan
+                           does not apply (BF16 interpolation, a row longer
+                           than ~3000 entries, a single-level hierarchy) the
+                           chain runs. */
+  double wait_limit_s;  /* bound on every wait of the persistent kernel (grid
+                           barriers, neighbour waits, shared-memory slots);
+                           past it the kernel stops and the call returns
+                           AFP_ERR_TIMEOUT (default 2 s, at most 60) */
+  int inject_barrier_stall; /* fault injection for tests: the first grid
+                           barrier of each persistent V-cycle waits for one
+                           arrival more than the grid has, so every wait runs
+                           out after wait_limit_s (default 0) */
 } afp_amg_opts;
 
 typedef struct afp_solve_info {

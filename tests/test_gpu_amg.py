@@ -152,27 +152,43 @@ def test_pcg_mixed_3d_hierarchy_keeps_fp64_iterations(ctx):
     assert it[1] <= it[0] + 2, it
 
 
-def test_fused_vcycle_matches_launch_chain(ctx):
-    """The FP32 V-cycle as one cooperative kernel does the launch chain's
-    arithmetic in the same order: same iterates bit for bit, with a small
-    fraction of the launches."""
+@pytest.mark.parametrize("wl_name", ["poisson3d_p1_32", "poisson2d_p1_128", "p2_3d_coef"])
+def test_streamed_vcycle_matches_launch_chain(ctx, wl_name):
+    """The FP32 V-cycle as one persistent streaming kernel does the launch
+    chain's arithmetic up to the order of each row's FP32 sum: stationary
+    V-cycle iterates agree to FP32 rounding, PCG takes the same number of
+    iterations (+-1) to the same direct solution, with one launch per V-cycle
+    instead of a chain."""
     from afepack_gb300 import workloads as W
     from afepack_gb300.amg import MIXED, AMGSolver
-    wl = W.poisson3d_p1(32)
+    from afepack_gb300.mesh import FESpace, cube_mesh
+    from afepack_gb300.workloads import Workload
+    if wl_name == "poisson3d_p1_32":
+        wl = W.poisson3d_p1(32)
+    elif wl_name == "poisson2d_p1_128":
+        wl = W.poisson2d_p1(128)
+    else:
+        mesh = cube_mesh(10, 0.15, 4)
+        sp = FESpace(mesh, 2)
+        rng = np.random.default_rng(3)
+        wl = Workload("t", sp, np.exp(rng.standard_normal(mesh.n_cell)), rng.standard_normal(sp.n_dof), 4, 4)
     _, K, b = system(ctx, wl)
+    xd = direct(K, b)
     runs = {}
-    for name, fused in (("chain", False), ("fused", True)):
+    for name, fused in (("chain", False), ("stream", True)):
         amg = AMGSolver(K, precision=MIXED, fused_vcycle=fused)
         x = np.zeros_like(b)
         n0 = ctx.launch_count()
         amg.solve(x, b, 0.0, 2)  # three V-cycles
         launches = ctx.launch_count() - n0
         xp, info = amg.pcg(b, 1e-10, 300)
-        runs[name] = (x, launches, xp, info["iterations"])
-    assert runs["fused"][1] * 5 < runs["chain"][1], (runs["fused"][1], runs["chain"][1])
-    assert np.array_equal(runs["fused"][0], runs["chain"][0])
-    assert runs["fused"][3] == runs["chain"][3]
-    assert np.array_equal(runs["fused"][2], runs["chain"][2])
+        assert info["converged"], (name, info)
+        assert np.linalg.norm(xp - xd) <= 1e-8 * np.linalg.norm(xd), name
+        runs[name] = (x, launches, info["iterations"])
+    assert runs["stream"][1] * 10 < runs["chain"][1], (runs["stream"][1], runs["chain"][1])
+    x0, x1 = runs["chain"][0], runs["stream"][0]
+    assert np.linalg.norm(x1 - x0) <= 1e-5 * np.linalg.norm(x0)
+    assert abs(runs["stream"][2] - runs["chain"][2]) <= 1, (runs["stream"][2], runs["chain"][2])
 
 
 @pytest.mark.parametrize("precision", [0, 1])

@@ -9,7 +9,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-BREAKDOWN, NOT_CONVERGED = 6, 5
+BREAKDOWN, NOT_CONVERGED, TIMEOUT = 6, 5, 8
 
 
 def _poisson(ctx, n=24, precision=0):
@@ -91,3 +91,23 @@ def test_one_poisoned_request_fails_alone_in_the_server(ctx):
     for (x, r), (xm, rm) in zip(solo, [out[0], out[2], out[3]]):
         assert r["status"] == 0 and rm["status"] == 0
         assert np.array_equal(x, xm)
+
+
+def test_stalled_grid_barrier_times_out_and_the_context_stays_usable(native, ctx):
+    """Fault injection on the GPU without a fault: the persistent V-cycle's
+    first grid barrier waits for one arrival more than the grid has (a count
+    that nothing completes); every bounded wait gives up after 50 ms, the
+    kernel returns, and the call reports AFP_ERR_TIMEOUT.  The same context
+    then solves normally."""
+    from afepack_gb300.amg import MIXED, AMGSolver
+    K, b, _ = _poisson(ctx, n=48)
+    amg = AMGSolver(K, precision=MIXED, fused_vcycle=True)
+    amg.opts.wait_limit_s = 0.05
+    amg.opts.inject_barrier_stall = 1
+    amg.reinit(K)
+    st, _, _ = _pcg_status(native, amg, b, 1e-10, 50)
+    assert st == TIMEOUT, native.afp_last_error()
+    assert b"bounded wait" in native.afp_last_error()
+    good = AMGSolver(K, precision=MIXED, fused_vcycle=True)
+    st, x, info = _pcg_status(native, good, b, 1e-10, 200)
+    assert st == 0 and info["converged"] == 1
