@@ -11,6 +11,8 @@
 // by binary searches on the sorted rows, which return the same entries.
 #include <algorithm>
 #include <cmath>
+#include <queue>
+#include <tuple>
 #include <cstdlib>
 #include <cstring>
 
@@ -278,7 +280,11 @@ void host_lazy_project(const HostCSR& M, HostCSR& P, HostCSR& Pt) {
   }
 }
 
-int host_color(const HostCSR& A, int max_colors, std::vector<int>& color) {
+namespace {
+
+// Greedy colouring in row order: row i takes the smallest colour that none of
+// its coupled, already coloured rows has (max_colors: the overflow class).
+int greedy_color(const HostCSR& A, int max_colors, std::vector<int>& color) {
   const int m = (int)A.m;
   color.assign(m, -1);
   std::vector<int> mark(max_colors + 1, -1);
@@ -298,6 +304,76 @@ int host_color(const HostCSR& A, int max_colors, std::vector<int>& color) {
     else used = std::max(used, c + 1);
   }
   return overflow ? max_colors + 1 : used;
+}
+
+// DSATUR (Brelaz): repeatedly colours the uncoloured row whose coupled rows
+// already show the most distinct colours (ties: more couplings, then the
+// lower row), with the smallest colour they leave free.  On mesh graphs it
+// finds colourings close to the fewest classes where row-order greedy
+// colouring needs about twice as many (the 3D Kuhn-split lattice: 4 against
+// 8).  Returns the colours used, or max_colors + 1 if some row found no free
+// colour below max_colors (it is then left in the overflow class).
+int dsatur_color(const HostCSR& A, int max_colors, std::vector<int>& color) {
+  const int m = (int)A.m;
+  // coupled neighbours (a nonzero entry either way), as adjacency lists
+  std::vector<int> off(m + 1, 0), adj;
+  adj.reserve(A.nnz());
+  for (int i = 0; i < m; ++i) {
+    for (int q = A.rowptr[i] + 1; q < A.rowptr[i + 1]; ++q) {
+      const int k = A.cols[q];
+      if (k == i || (A.vals[q] == 0.0 && entry(A, k, i) == 0.0)) continue;
+      adj.push_back(k);
+    }
+    off[i + 1] = (int)adj.size();
+  }
+  color.assign(m, -1);
+  std::vector<uint64_t> seen(m, 0);  // colours present among coupled rows (max_colors <= 63)
+  std::vector<int> sat(m, 0);
+  using Key = std::tuple<int, int, int>;  // (saturation, couplings, -row)
+  std::priority_queue<Key> pq;
+  for (int i = 0; i < m; ++i) pq.push(Key(0, off[i + 1] - off[i], -i));
+  int used = 0;
+  bool overflow = false;
+  while (!pq.empty()) {
+    const Key top = pq.top();
+    pq.pop();
+    const int i = -std::get<2>(top);
+    if (color[i] >= 0 || std::get<0>(top) != sat[i]) continue;  // stale entry
+    int c = 0;
+    while (c < max_colors && ((seen[i] >> c) & 1u)) ++c;
+    color[i] = c;
+    if (c == max_colors) {
+      overflow = true;
+      continue;
+    }
+    used = std::max(used, c + 1);
+    for (int q = off[i]; q < off[i + 1]; ++q) {
+      const int k = adj[q];
+      if (color[k] >= 0 || ((seen[k] >> c) & 1u)) continue;
+      seen[k] |= uint64_t(1) << c;
+      ++sat[k];
+      pq.push(Key(sat[k], off[k + 1] - off[k], -k));
+    }
+  }
+  return overflow ? max_colors + 1 : used;
+}
+
+}  // namespace
+
+int host_color(const HostCSR& A, int max_colors, std::vector<int>& color) {
+  const int greedy = greedy_color(A, max_colors, color);
+  // A level that needs the overflow class keeps the row-order classes (each
+  // a maximal independent set of the rows left, which keeps the l1-Jacobi
+  // remainder small); otherwise DSATUR is tried for fewer classes, i.e. fewer
+  // dependent steps per Gauss-Seidel sweep.
+  if (greedy > max_colors || greedy <= 2 || max_colors > 63) return greedy;
+  std::vector<int> ds;
+  const int k = dsatur_color(A, max_colors, ds);
+  if (k < greedy) {
+    color.swap(ds);
+    return k;
+  }
+  return greedy;
 }
 
 }  // namespace afp

@@ -62,6 +62,7 @@ constexpr int kTailSeg = (kBlobMax / 8) / 4 * 4;  // floats of hi (and of lo) pe
 constexpr int kRingBytes = kSlots * kSlotBytes;
 constexpr int kPhaseBits = 12;                    // progress flags: epoch << 12 | phase
 constexpr int kNbLevels = 16;                     // levels whose neighbour lists sit in shared memory
+constexpr int kTailRows = 128;                    // dense tail rows per CTA (row partials in shared memory)
 
 enum Op : int { OP_START = 0, OP_GS, OP_JAC, OP_RES, OP_RESTRICT, OP_TAIL, OP_TAIL_DIAG, OP_PROLONG, OP_FINISH };
 
@@ -124,6 +125,7 @@ struct Shared {
   unsigned epoch;
   int nnb[kNbLevels];       // this CTA's neighbour CTAs per level (count, list)
   int nbr[kNbLevels][32];
+  float2 tailp[kTailRows][kConsumerWarps];  // per tail row, each warp's double-float partial
 };
 
 // Raises the error word (with `where`, the phase that gave up) and the
@@ -354,28 +356,27 @@ __device__ void tail_tile(const StreamLevel& Lt, const char* __restrict__ slot, 
   }
 }
 
-// After a tail row's last segment: (sh, sl) reduced over all consumers in a
-// fixed order; every consumer thread calls it (it holds consumer barriers).
-__device__ void tail_row_end(const StreamLevel& Lt, int row, float& sh, float& sl, Shared& s) {
+// After a tail row's last segment: each warp reduces its lanes' (sh, sl) and
+// parks the pair in shared memory (no CTA-wide wait per row).
+__device__ __forceinline__ void tail_row_end(int rl, float& sh, float& sl, Shared& s) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
     const float oh = __shfl_xor_sync(0xffffffffu, sh, off);
     const float ol = __shfl_xor_sync(0xffffffffu, sl, off);
     df_add(sh, sl, oh, ol);
   }
-  const int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) {
-    s.red[2 * w] = sh;
-    s.red[2 * w + 1] = sl;
-  }
-  consumers_sync();
-  if (threadIdx.x == 0) {
-    float h = s.red[0], l = s.red[1];
-    for (int i = 1; i < kConsumerWarps; ++i) df_add(h, l, s.red[2 * i], s.red[2 * i + 1]);
-    Lt.x[row] = __fadd_rn(h, l);
-  }
-  consumers_sync();
+  if ((threadIdx.x & 31) == 0) s.tailp[rl][threadIdx.x >> 5] = make_float2(sh, sl);
   sh = sl = 0.f;
+}
+
+// After the CTA's last tail row: every row's warp pairs summed in warp order.
+__device__ void tail_rows_finish(const StreamLevel& Lt, int row0, int nrows, Shared& s) {
+  consumers_sync();
+  for (int rl = threadIdx.x; rl < nrows; rl += kConsumers) {
+    float h = s.tailp[rl][0].x, l = s.tailp[rl][0].y;
+    for (int w = 1; w < kConsumerWarps; ++w) df_add(h, l, s.tailp[rl][w].x, s.tailp[rl][w].y);
+    Lt.x[row0 + rl] = __fadd_rn(h, l);
+  }
 }
 
 __global__ void __launch_bounds__(kThreads, 1) k_vcycle_stream(StreamArgs a) {
@@ -462,6 +463,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_vcycle_stream(StreamArgs a) {
           const StreamLevel Ln = a.L[P.level + 1 <= a.t ? P.level + 1 : P.level];
           int i = P.tile0;
           const int end = P.tile0 + P.ntiles;
+          const int tail_row0 = (P.op == OP_TAIL && P.ntiles > 0) ? tiles[P.tile0].row0 : 0;
+          int tail_rows = 0;
           while (i < end) {
             // a thread whose wait fails (abort) skips the work but keeps every
             // consumer barrier of the schedule; the next wait stops all
@@ -497,9 +500,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_vcycle_stream(StreamArgs a) {
             __syncwarp();
             if ((threadIdx.x & 31) == 0)
               for (int j = 0; j < nw; ++j) mbar_arrive(&s.empty[(i + j) % kSlots]);
-            if (tail && ((tmeta >> 10) & 1)) tail_row_end(L, trow, sh, sl, s);
+            if (tail && ((tmeta >> 10) & 1)) {
+              tail_row_end(trow - tail_row0, sh, sl, s);
+              tail_rows = trow - tail_row0 + 1;
+            }
             i += nw;
           }
+          if (P.op == OP_TAIL) tail_rows_finish(L, tail_row0, tail_rows, s);
           break;
         }
       }
@@ -657,6 +664,7 @@ void fused_build(afp_amg* h) {
   AFP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vcycle_stream, kThreads, kRingBytes + 128));
   if (per_sm < 1) return;
   const int G = ctx->sm_count;
+  if (h->tail_dense && (h->lv[t].n + G - 1) / G > kTailRows) return;
   auto F = std::make_unique<FusedPlan>();
   F->grid = G;
   // Row runs: each colour class of a smoothed level is split into G runs of
