@@ -778,7 +778,7 @@ void afp_amg_default_opts(afp_amg_opts* o) {
   o->symmetric = 1;
   o->coarse_colors = 4;
   o->interp_bf16 = 0;
-  o->fused_vcycle = 1;
+  o->fused_vcycle = 0;
   o->wait_limit_s = 2.0;
   o->inject_barrier_stall = 0;
 }
