@@ -43,119 +43,6 @@ __device__ __forceinline__ float as<float, __nv_bfloat16>(__nv_bfloat16 v) {
 __device__ __forceinline__ int64_t warp_id() { return ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
 __device__ __forceinline__ int64_t n_warps() { return ((int64_t)gridDim.x * blockDim.x) >> 5; }
 
-// y = A x or y += A x over n x k blocks
-template <int KPL, class V, class X, bool ADD>
-__global__ void k_spmm(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci, const V* __restrict__ va,
-                       const X* __restrict__ x, X* __restrict__ y, int k) {
-  using A = typename AccT<X>::type;
-  const int lane = threadIdx.x & 31;
-  for (int64_t row = warp_id(); row < m; row += n_warps()) {
-    A acc[KPL];
-#pragma unroll
-    for (int q = 0; q < KPL; ++q) acc[q] = 0;
-    for (int j = rp[row]; j < rp[row + 1]; ++j) {
-      const A a = as<A>(va[j]);
-      const X* xr = x + (int64_t)ci[j] * k;
-#pragma unroll
-      for (int q = 0; q < KPL; ++q) {
-        const int c = lane + 32 * q;
-        if (c < k) acc[q] += a * (A)xr[c];
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < KPL; ++q) {
-      const int c = lane + 32 * q;
-      if (c < k) {
-        X* o = y + row * k + c;
-        *o = ADD ? (X)((A)*o + acc[q]) : (X)acc[q];
-      }
-    }
-  }
-}
-
-template <int KPL, class X>
-__global__ void k_residual_m(int64_t m, const int* __restrict__ rp, const int* __restrict__ ci,
-                             const X* __restrict__ va, const X* __restrict__ x, const X* __restrict__ r,
-                             X* __restrict__ out, int k) {
-  using A = typename AccT<X>::type;
-  const int lane = threadIdx.x & 31;
-  for (int64_t row = warp_id(); row < m; row += n_warps()) {
-    A acc[KPL];
-#pragma unroll
-    for (int q = 0; q < KPL; ++q) acc[q] = 0;
-    for (int j = rp[row]; j < rp[row + 1]; ++j) {
-      const A a = (A)va[j];
-      const X* xr = x + (int64_t)ci[j] * k;
-#pragma unroll
-      for (int q = 0; q < KPL; ++q) {
-        const int c = lane + 32 * q;
-        if (c < k) acc[q] += a * (A)xr[c];
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < KPL; ++q) {
-      const int c = lane + 32 * q;
-      if (c < k) out[row * k + c] = (X)((A)r[row * k + c] - acc[q]);
-    }
-  }
-}
-
-template <int KPL, class X>
-__global__ void k_gs_class_m(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
-                             const X* __restrict__ va, X* __restrict__ x, const X* __restrict__ r, int k) {
-  using A = typename AccT<X>::type;
-  const int lane = threadIdx.x & 31;
-  for (int64_t row = r0 + warp_id(); row < r1; row += n_warps()) {
-    A acc[KPL];
-#pragma unroll
-    for (int q = 0; q < KPL; ++q) acc[q] = 0;
-    const int d = rp[row];
-    for (int j = d + 1; j < rp[row + 1]; ++j) {
-      const A a = (A)va[j];
-      const X* xr = x + (int64_t)ci[j] * k;
-#pragma unroll
-      for (int q = 0; q < KPL; ++q) {
-        const int c = lane + 32 * q;
-        if (c < k) acc[q] += a * (A)xr[c];
-      }
-    }
-    const A diag = (A)va[d];
-#pragma unroll
-    for (int q = 0; q < KPL; ++q) {
-      const int c = lane + 32 * q;
-      if (c < k) x[row * k + c] = (X)(((A)r[row * k + c] - acc[q]) / diag);
-    }
-  }
-}
-
-template <int KPL, class X>
-__global__ void k_jacobi_l1_m(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
-                              const X* __restrict__ va, const X* __restrict__ x, const X* __restrict__ r,
-                              const X* __restrict__ d, X* __restrict__ tmp, int k) {
-  using A = typename AccT<X>::type;
-  const int lane = threadIdx.x & 31;
-  for (int64_t row = r0 + warp_id(); row < r1; row += n_warps()) {
-    A acc[KPL];
-#pragma unroll
-    for (int q = 0; q < KPL; ++q) acc[q] = 0;
-    for (int j = rp[row]; j < rp[row + 1]; ++j) {
-      const A a = (A)va[j];
-      const X* xr = x + (int64_t)ci[j] * k;
-#pragma unroll
-      for (int q = 0; q < KPL; ++q) {
-        const int c = lane + 32 * q;
-        if (c < k) acc[q] += a * (A)xr[c];
-      }
-    }
-    const A dd = (A)d[row - r0];
-#pragma unroll
-    for (int q = 0; q < KPL; ++q) {
-      const int c = lane + 32 * q;
-      if (c < k) tmp[(row - r0) * k + c] = (X)((A)x[row * k + c] + ((A)r[row * k + c] - acc[q]) / dd);
-    }
-  }
-}
-
 template <class X>
 __global__ void k_copy(int64_t n, const X* __restrict__ s, X* __restrict__ d) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -186,28 +73,159 @@ __global__ void k_dense_gemm(int64_t n, const X* __restrict__ M, const X* __rest
   }
 }
 
-// FP32 V-cycle tail: X = (hi + lo) R with a double-float pair per column
-// (the single-column kernel's accumulation, see df32.cuh)
-template <int KPL>
-__global__ void k_dense_gemm_df(int64_t n, int64_t ld, const float* __restrict__ hi, const float* __restrict__ lo,
-                                const float* __restrict__ r, float* __restrict__ x, int k) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t row = warp_id(); row < n; row += n_warps()) {
-    float sh[KPL], sl[KPL];
+// --------------------------------------------------- V-cycle row kernels
+// One kernel for every row operation of the batched V-cycle on rows [r0, r1)
+// of an n x k block: a sub-warp of W lanes (a power of two, W >= k up to 32)
+// takes one row, lane l owning columns l, l + W, ... (KPL of them).  The
+// row's (column, value) pairs are loaded W at a time, one per lane, and
+// broadcast with shuffles; the gathers of x rows they address are issued four
+// entries ahead (unrolled), so a row costs about two dependent memory round
+// trips whatever its length.
+enum RowOp { RO_SPMM = 0, RO_SPMM_ADD, RO_RES, RO_GS, RO_JAC };
+
+template <int W, int KPL, class V, class X, int OP>
+__global__ void k_rows_m(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
+                         const V* __restrict__ va, const X* x, X* y, const X* __restrict__ r,
+                         const X* __restrict__ d, int k) {
+  using A = typename AccT<X>::type;
+  const int64_t row = r0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / W;
+  if (row >= r1) return;  // a whole sub-warp leaves together
+  const int lane = threadIdx.x & (W - 1);
+  const unsigned mask = W >= 32 ? 0xffffffffu : (((1u << W) - 1u) << ((threadIdx.x & 31) & ~(W - 1)));
+  A acc[KPL];
 #pragma unroll
-    for (int q = 0; q < KPL; ++q) sh[q] = sl[q] = 0.f;
-    for (int64_t j = 0; j < n; ++j) {
-      const float a = hi[row * ld + j], b = lo[row * ld + j];
+  for (int q = 0; q < KPL; ++q) acc[q] = 0;
+  int b = rp[row];
+  const int e = rp[row + 1];
+  A diag = 1;
+  if (OP == RO_GS) {  // the diagonal is the row's first entry
+    diag = as<A>(va[b]);
+    ++b;
+  }
+  if (W == 1) {
+#pragma unroll 4
+    for (int j = b; j < e; ++j) {
+      const A val = as<A>(va[j]);
+      const X* xr = x + (int64_t)ci[j] * k;
 #pragma unroll
-      for (int q = 0; q < KPL; ++q) {
-        const int c = lane + 32 * q;
-        if (c < k) df_add_prod(sh[q], sl[q], a, b, r[j * k + c]);
+      for (int q = 0; q < KPL; ++q)
+        if (q < k) acc[q] += val * (A)xr[q];
+    }
+  } else {
+    for (int base = b; base < e; base += W) {
+      const int my = base + lane;
+      const int cc = my < e ? ci[my] : 0;
+      const A vv = my < e ? as<A>(va[my]) : A(0);
+      const int cnt = min(W, e - base);
+#pragma unroll 4
+      for (int jj = 0; jj < cnt; ++jj) {
+        const int col = __shfl_sync(mask, cc, jj, W);
+        const A val = __shfl_sync(mask, vv, jj, W);
+        const X* xr = x + (int64_t)col * k;
+#pragma unroll
+        for (int q = 0; q < KPL; ++q) {
+          const int c = lane + W * q;
+          if (c < k) acc[q] += val * (A)xr[c];
+        }
       }
     }
+  }
 #pragma unroll
-    for (int q = 0; q < KPL; ++q) {
-      const int c = lane + 32 * q;
-      if (c < k) x[row * k + c] = __fadd_rn(sh[q], sl[q]);
+  for (int q = 0; q < KPL; ++q) {
+    const int c = lane + W * q;
+    if (c >= k) continue;
+    const int64_t o = row * k + c;
+    if (OP == RO_SPMM) y[o] = (X)acc[q];
+    else if (OP == RO_SPMM_ADD) y[o] = (X)((A)y[o] + acc[q]);
+    else if (OP == RO_RES) y[o] = (X)((A)r[o] - acc[q]);
+    else if (OP == RO_GS) y[o] = (X)(((A)r[o] - acc[q]) / diag);
+    else y[(row - r0) * k + c] = (X)((A)x[o] + ((A)r[o] - acc[q]) / (A)d[row - r0]);  // RO_JAC into tmp
+  }
+}
+
+// Launches k_rows_m with W = the smallest power of two >= k (at most 32) and
+// KPL = columns per lane.
+template <class V, class X, int OP>
+void rows_m(const afp_context* ctx, int64_t r0, int64_t r1, const int* rp, const int* ci, const V* va, const X* x,
+            X* y, const X* r, const X* d, int k, const char* what) {
+  if (r1 <= r0) return;
+  auto go = [&](auto Wc, auto Kc) {
+    constexpr int W = decltype(Wc)::value, KPL = decltype(Kc)::value;
+    k_rows_m<W, KPL, V, X, OP><<<grid_for((r1 - r0) * W, 256), 256, 0, ctx->stream>>>(r0, r1, rp, ci, va, x, y, r, d,
+                                                                                     k);
+  };
+  using I1 = std::integral_constant<int, 1>;
+  using I2 = std::integral_constant<int, 2>;
+  if (k == 1) go(I1(), I1());
+  else if (k == 2) go(std::integral_constant<int, 2>(), I1());
+  else if (k <= 4) go(std::integral_constant<int, 4>(), I1());
+  else if (k <= 8) go(std::integral_constant<int, 8>(), I1());
+  else if (k <= 16) go(std::integral_constant<int, 16>(), I1());
+  else if (k <= 32) go(std::integral_constant<int, 32>(), I1());
+  else go(std::integral_constant<int, 32>(), I2());
+  check_launch(ctx, what);
+}
+
+// X = (hi + lo) R for the dense tail: an n x n double-float pair (rows of
+// stride ld) times an n x k FP32 block, accumulated in double-float.  A block
+// of 256 threads computes TR rows x k columns; R and the rows' hi/lo are
+// staged in shared memory TJ columns at a time.  When there are fewer outputs
+// than threads, S threads share an output, each taking every S-th inner
+// index, and their pairs are summed in a fixed order at the end.
+template <int TR>
+__global__ void __launch_bounds__(256) k_tail_gemm_df(int64_t n, int64_t ld, const float* __restrict__ hi,
+                                                       const float* __restrict__ lo, const float* __restrict__ R,
+                                                       float* __restrict__ X, int k) {
+  constexpr int BT = 256, TJ = 64, MAXO = TR * MAXK / BT;
+  __shared__ float sR[TJ * MAXK];
+  __shared__ float sH[TR * TJ], sL[TR * TJ];
+  __shared__ float2 red[BT];
+  const int64_t row0 = (int64_t)blockIdx.x * TR;
+  const int O = TR * k;
+  const int S = O >= BT ? 1 : BT / O;
+  const int per = BT / S;  // outputs in flight at once
+  const int tid = threadIdx.x, ob = tid / S, s = tid % S;
+  const bool busy = tid < per * S;
+  float sh[MAXO > 0 ? MAXO : 1], sl[MAXO > 0 ? MAXO : 1];
+#pragma unroll
+  for (int q = 0; q < (MAXO > 0 ? MAXO : 1); ++q) sh[q] = sl[q] = 0.f;
+  for (int64_t j0 = 0; j0 < n; j0 += TJ) {  // columns [n, ld) of hi / lo are zeros: stop at n (R has n rows)
+    const int tj = (int)(n - j0 < TJ ? n - j0 : TJ);
+    __syncthreads();
+    for (int t = tid; t < tj * k; t += BT) sR[t] = R[j0 * k + t];
+    for (int t = tid; t < TR * TJ; t += BT) {
+      const int rr = t / TJ, jj = t % TJ;
+      const bool on = row0 + rr < n && jj < tj;
+      sH[t] = on ? hi[(row0 + rr) * ld + j0 + jj] : 0.f;
+      sL[t] = on ? lo[(row0 + rr) * ld + j0 + jj] : 0.f;
+    }
+    __syncthreads();
+    if (busy) {
+#pragma unroll
+      for (int q = 0; q < (MAXO > 0 ? MAXO : 1); ++q) {
+        const int o = ob + q * per;
+        if (o >= O) break;
+        const int rr = o / k, c = o % k;
+        for (int jj = s; jj < tj; jj += S) df_add_prod(sh[q], sl[q], sH[rr * TJ + jj], sL[rr * TJ + jj], sR[jj * k + c]);
+      }
+    }
+  }
+  if (S > 1) {
+    red[tid] = make_float2(sh[0], sl[0]);
+    __syncthreads();
+    if (busy && s == 0 && ob < O) {
+      float h = red[tid].x, l = red[tid].y;
+      for (int u = 1; u < S; ++u) df_add(h, l, red[tid + u].x, red[tid + u].y);
+      const int rr = ob / k, c = ob % k;
+      if (row0 + rr < n) X[(row0 + rr) * k + c] = __fadd_rn(h, l);
+    }
+  } else if (busy) {
+#pragma unroll
+    for (int q = 0; q < (MAXO > 0 ? MAXO : 1); ++q) {
+      const int o = ob + q * per;
+      if (o >= O) break;
+      const int rr = o / k, c = o % k;
+      if (row0 + rr < n) X[(row0 + rr) * k + c] = __fadd_rn(sh[q], sl[q]);
     }
   }
 }
@@ -412,75 +430,67 @@ template <class X, class PV>
 void vcycle_m(afp_amg* h, MultiState& S) {
   const afp_context* ctx = h->ctx;
   const int k = S.k, t = h->t;
-  with_kpl(k, [&](auto KPLc) {
-    constexpr int KPL = decltype(KPLc)::value;
-    auto smooth = [&](int l, X* x, const X* r, bool backward) {
-      const Level& L = h->lv[l];
-      CSRView<X> A = L.A<X>();
-      const int K = (int)L.cls.size() - 1;
-      for (int s = 0; s < h->opts.smooth_step; ++s)
-        for (int q = 0; q < K; ++q) {
-          const int c = backward ? K - 1 - q : q;
-          const int64_t r0 = L.cls[c], r1 = L.cls[c + 1];
-          if (r1 <= r0) continue;
-          if (L.overflow && c == K - 1) {
-            const X* d;
-            if constexpr (std::is_same<X, double>::value) d = L.l1d.get();
-            else d = L.l1d32.get();
-            X* tmp = blk<X>(S, 2, l);
-            k_jacobi_l1_m<KPL, X><<<rows_grid(ctx, r1 - r0), BLK, 0, ctx->stream>>>(r0, r1, A.rowptr, A.cols, A.vals,
-                                                                                   x, r, d, tmp, k);
-            check_launch(ctx, "mrhs l1-jacobi");
-            k_copy<X><<<grid_for((r1 - r0) * k, BLK), BLK, 0, ctx->stream>>>((r1 - r0) * k, tmp, x + r0 * k);
-            check_launch(ctx, "mrhs copy");
-          } else {
-            k_gs_class_m<KPL, X><<<rows_grid(ctx, r1 - r0), BLK, 0, ctx->stream>>>(r0, r1, A.rowptr, A.cols, A.vals,
-                                                                                  x, r, k);
-            check_launch(ctx, "mrhs gauss-seidel class");
-          }
+  auto smooth = [&](int l, X* x, const X* r, bool backward) {
+    const Level& L = h->lv[l];
+    CSRView<X> A = L.A<X>();
+    const int K = (int)L.cls.size() - 1;
+    for (int s = 0; s < h->opts.smooth_step; ++s)
+      for (int q = 0; q < K; ++q) {
+        const int c = backward ? K - 1 - q : q;
+        const int64_t r0 = L.cls[c], r1 = L.cls[c + 1];
+        if (r1 <= r0) continue;
+        if (L.overflow && c == K - 1) {
+          const X* d;
+          if constexpr (std::is_same<X, double>::value) d = L.l1d.get();
+          else d = L.l1d32.get();
+          X* tmp = blk<X>(S, 2, l);
+          rows_m<X, X, RO_JAC>(ctx, r0, r1, A.rowptr, A.cols, A.vals, x, tmp, r, d, k, "mrhs l1-jacobi");
+          k_copy<X><<<grid_for((r1 - r0) * k, BLK), BLK, 0, ctx->stream>>>((r1 - r0) * k, tmp, x + r0 * k);
+          check_launch(ctx, "mrhs copy");
+        } else {
+          rows_m<X, X, RO_GS>(ctx, r0, r1, A.rowptr, A.cols, A.vals, x, x, r, nullptr, k, "mrhs gauss-seidel class");
         }
-    };
-    for (int l = 0; l < t; ++l) {
-      Level& L = h->lv[l];
-      X* x = blk<X>(S, 0, l);
-      const X* r = blk<X>(S, 1, l);
-      k_zero_m<X><<<grid_for(L.n * k, BLK), BLK, 0, ctx->stream>>>(L.n * k, x);
-      check_launch(ctx, "mrhs zero");
-      smooth(l, x, r, false);
-      CSRView<X> A = L.A<X>();
-      k_residual_m<KPL, X><<<rows_grid(ctx, L.n), BLK, 0, ctx->stream>>>(L.n, A.rowptr, A.cols, A.vals, x, r,
-                                                                        blk<X>(S, 2, l), k);
-      check_launch(ctx, "mrhs residual");
-      const PV* pv = p_vals<PV>(L);
-      const int64_t nc = h->lv[l + 1].n;
-      k_spmm<KPL, PV, X, false><<<rows_grid(ctx, nc), BLK, 0, ctx->stream>>>(nc, L.prp.get(), L.pci.get(), pv,
-                                                                            blk<X>(S, 2, l), blk<X>(S, 1, l + 1), k);
-      check_launch(ctx, "mrhs restriction");
-    }
-    const Level& T = h->lv[t];
-    if (h->tail_dense) {
-      if constexpr (std::is_same<X, double>::value)
+      }
+  };
+  for (int l = 0; l < t; ++l) {
+    Level& L = h->lv[l];
+    X* x = blk<X>(S, 0, l);
+    const X* r = blk<X>(S, 1, l);
+    k_zero_m<X><<<grid_for(L.n * k, BLK), BLK, 0, ctx->stream>>>(L.n * k, x);
+    check_launch(ctx, "mrhs zero");
+    smooth(l, x, r, false);
+    CSRView<X> A = L.A<X>();
+    rows_m<X, X, RO_RES>(ctx, 0, L.n, A.rowptr, A.cols, A.vals, x, blk<X>(S, 2, l), r, nullptr, k, "mrhs residual");
+    const int64_t nc = h->lv[l + 1].n;
+    rows_m<PV, X, RO_SPMM>(ctx, 0, nc, L.prp.get(), L.pci.get(), p_vals<PV>(L), blk<X>(S, 2, l), blk<X>(S, 1, l + 1),
+                           nullptr, nullptr, k, "mrhs restriction");
+  }
+  const Level& T = h->lv[t];
+  if (h->tail_dense) {
+    if constexpr (std::is_same<X, double>::value) {
+      with_kpl(k, [&](auto KPLc) {
+        constexpr int KPL = decltype(KPLc)::value;
         k_dense_gemm<KPL, X><<<rows_grid(ctx, T.n), BLK, 0, ctx->stream>>>(T.n, h->tail_inv.get(), blk<X>(S, 1, t),
                                                                           blk<X>(S, 0, t), k);
-      else
-        k_dense_gemm_df<KPL><<<rows_grid(ctx, T.n), BLK, 0, ctx->stream>>>(T.n, h->tail_ld, h->tail_hi.get(), h->tail_lo.get(),
-                                                                          blk<X>(S, 1, t), blk<X>(S, 0, t), k);
-      check_launch(ctx, "mrhs dense tail");
+      });
     } else {
-      CSRView<X> A = T.A<X>();
-      k_diag_solve_m<X><<<grid_for(T.n * k, BLK), BLK, 0, ctx->stream>>>(T.n, A.rowptr, A.vals, blk<X>(S, 1, t),
-                                                                         blk<X>(S, 0, t), k);
-      check_launch(ctx, "mrhs diagonal tail");
+      constexpr int TR = 16;
+      k_tail_gemm_df<TR><<<(unsigned)((T.n + TR - 1) / TR), 256, 0, ctx->stream>>>(
+          T.n, h->tail_ld, h->tail_hi.get(), h->tail_lo.get(), blk<X>(S, 1, t), blk<X>(S, 0, t), k);
     }
-    for (int l = t - 1; l >= 0; --l) {
-      Level& L = h->lv[l];
-      const PV* tv = pt_vals<PV>(L);
-      k_spmm<KPL, PV, X, true><<<rows_grid(ctx, L.n), BLK, 0, ctx->stream>>>(L.n, L.trp.get(), L.tci.get(), tv,
-                                                                            blk<X>(S, 0, l + 1), blk<X>(S, 0, l), k);
-      check_launch(ctx, "mrhs prolongation");
-      smooth(l, blk<X>(S, 0, l), blk<X>(S, 1, l), h->opts.symmetric != 0);
-    }
-  });
+    check_launch(ctx, "mrhs dense tail");
+  } else {
+    CSRView<X> A = T.A<X>();
+    k_diag_solve_m<X><<<grid_for(T.n * k, BLK), BLK, 0, ctx->stream>>>(T.n, A.rowptr, A.vals, blk<X>(S, 1, t),
+                                                                       blk<X>(S, 0, t), k);
+    check_launch(ctx, "mrhs diagonal tail");
+  }
+  for (int l = t - 1; l >= 0; --l) {
+    Level& L = h->lv[l];
+    rows_m<PV, X, RO_SPMM_ADD>(ctx, 0, L.n, L.trp.get(), L.tci.get(), pt_vals<PV>(L), blk<X>(S, 0, l + 1),
+                               blk<X>(S, 0, l), nullptr, nullptr, k, "mrhs prolongation");
+    smooth(l, blk<X>(S, 0, l), blk<X>(S, 1, l), h->opts.symmetric != 0);
+  }
 }
 
 void ensure_state(afp_amg* h, int k) {
@@ -593,11 +603,10 @@ bool pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, doubl
   S.active.upload(act.data(), k);
   const CSRView<double> A = L0.A<double>();
   const unsigned rg = std::min<unsigned>(RED_GRID, rows_grid(ctx, n));
+  rows_m<double, double, RO_RES>(ctx, 0, n, A.rowptr, A.cols, A.vals, S.Xs.get(), S.Rs.get(), S.B.get(), nullptr, k,
+                                 "mrhs residual");
   with_kpl(k, [&](auto KPLc) {
     constexpr int KPL = decltype(KPLc)::value;
-    k_residual_m<KPL, double><<<rows_grid(ctx, n), BLK, 0, ctx->stream>>>(n, A.rowptr, A.cols, A.vals, S.Xs.get(),
-                                                                          S.B.get(), S.Rs.get(), k);
-    check_launch(ctx, "mrhs residual");
     k_col_dot<KPL><<<rg, BLK, 0, ctx->stream>>>(n, S.B.get(), S.B.get(), k, partials, sc + 4 * MAXK);
     check_launch(ctx, "mrhs dot");
     k_col_dot<KPL><<<rg, BLK, 0, ctx->stream>>>(n, S.Rs.get(), S.Rs.get(), k, partials, sc + 2 * MAXK);
