@@ -73,6 +73,10 @@ class RequestResult(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class BatchOpts(C.Structure):
+    _fields_ = [("width", C.c_int), ("tol", C.c_double), ("maxit", C.c_int)]
+
+
 class ServerStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64), ("p50_seconds", C.c_double),
                 ("p99_seconds", C.c_double), ("solves_per_second", C.c_double), ("budget_bytes", C.c_int64),
@@ -132,9 +136,17 @@ SIGNATURES = {
     "afp_server_get_stats": [C.c_void_p, C.POINTER(ServerStats)],
     "afp_server_reset_stats": [C.c_void_p],
     "afp_server_destroy": [C.c_void_p],
+    "afp_batch_default_opts": [C.POINTER(BatchOpts)],
+    "afp_batch_server_create": [C.c_void_p, C.POINTER(BatchOpts), c_void_pp],
+    "afp_batch_server_submit": [C.c_void_p, C.c_void_p, c_i64p],
+    "afp_batch_server_wait": [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(RequestResult)],
+    "afp_batch_server_get_stats": [C.c_void_p, C.POINTER(ServerStats)],
+    "afp_batch_server_reset_stats": [C.c_void_p],
+    "afp_batch_server_destroy": [C.c_void_p],
 }
 _RESTYPES = {"afp_version": C.c_int, "afp_status_string": C.c_char_p, "afp_last_error": C.c_char_p,
-             "afp_amg_default_opts": None, "afp_host_free": None, "afp_server_default_opts": None}
+             "afp_amg_default_opts": None, "afp_host_free": None, "afp_server_default_opts": None,
+             "afp_batch_default_opts": None}
 
 _lib = None
 

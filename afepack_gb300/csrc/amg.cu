@@ -917,7 +917,12 @@ afp_status afp_amg_solve(afp_amg* h, double* x, const double* r, double tol, int
 
 afp_status afp_amg_time_kernel(afp_amg* h, int kind, int level, int reps, double* ms, double* bytes) {
   return guarded([&] {
-    AFP_REQUIRE(h && ms && bytes && reps > 0 && kind >= 0 && kind <= 3, AFP_ERR_INVALID, "bad argument");
+    AFP_REQUIRE(h && ms && bytes && reps > 0 && kind >= 0 && kind <= 5, AFP_ERR_INVALID, "bad argument");
+    if (kind >= 4) {
+      bind(h->ctx);
+      time_multi(h, kind, level, reps, ms, bytes);
+      return;
+    }
     AFP_REQUIRE(level >= 0 && level < std::max(1, h->t), AFP_ERR_INVALID, "level is not a smoothed level");
     afp_context* ctx = h->ctx;
     bind(ctx);

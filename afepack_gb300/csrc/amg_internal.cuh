@@ -196,6 +196,7 @@ struct afp_amg {
 namespace afp {
 // Batched CG over nrhs columns (mrhs.cu); false when a column stopped at
 // the iteration limit above the tolerance.
+void time_multi(afp_amg* h, int kind, int level, int reps, double* ms, double* bytes);
 bool pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, double tol, int maxit,
                afp_solve_info* info);
 // Streamed FP32 V-cycle (vcycle_stream.cu): plan from the solve layout

@@ -10,7 +10,16 @@
 // CG keeps its recurrences per column: column scalars live on the device, a
 // column stops updating once its relative residual meets the tolerance, and
 // the iteration ends when every column has.
+#include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
 
 #include "amg_internal.cuh"
 #include "df32.cuh"
@@ -696,4 +705,407 @@ bool pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, doubl
   return true;
 }
 
+}  // namespace afp
+
+// ==================================================================== serving
+// Continuous batching of solves against one resident hierarchy.
+//
+// The server owns the hierarchy's batched CG state at a fixed width of k
+// columns; each column is an execution slot.  One driver thread runs CG
+// iterations over all k columns (one batched V-cycle, one FP64 A p, the
+// column recurrences) and, between two iterations, admits queued requests
+// into free columns and retires the ones that converged, so requests arrive
+// and leave while others are in flight.  A request's column starts with
+// x = 0, r = b, p = 0 and an old r.z of 1, so its first step is the plain
+// CG start p = z.  Free columns hold r = p = 0 and are masked out of every
+// update; the batched kernels are deterministic and each column's arithmetic
+// uses only its own entries, so a request's solution does not depend on the
+// other columns.
+namespace afp {
+namespace {
+
+// column c of the solve-order block <- src[perm[i]] (b), x = 0, r = b, p = 0
+__global__ void k_col_admit(int64_t n, int k, int c, const int* __restrict__ perm, const double* __restrict__ src,
+                            double* __restrict__ B, double* __restrict__ X, double* __restrict__ R,
+                            double* __restrict__ P) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = src[perm[i]];
+  const int64_t o = i * k + c;
+  B[o] = v;
+  X[o] = 0.0;
+  R[o] = v;
+  P[o] = 0.0;
+}
+
+// dst[perm[i]] = X column c; then r = p = 0 in that column (a free slot)
+__global__ void k_col_retire(int64_t n, int k, int c, const int* __restrict__ perm, const double* __restrict__ X,
+                             double* __restrict__ dst, double* __restrict__ R, double* __restrict__ P) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t o = i * k + c;
+  dst[perm[i]] = X[o];
+  R[o] = 0.0;
+  P[o] = 0.0;
+}
+
+}  // namespace
+}  // namespace afp
+
+struct afp_batch_server {
+  afp_amg* amg = nullptr;
+  afp_batch_opts opts{};
+  struct Req {
+    int64_t ticket = 0;
+    std::vector<double> b, x;
+    afp_request_result res{};
+    std::chrono::steady_clock::time_point t_submit, t_admit;
+    bool done = false;
+  };
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Req*> queue;
+  std::unordered_map<int64_t, std::unique_ptr<Req>> reqs;
+  std::thread driver;
+  bool stop = false;
+  int64_t next_ticket = 1;
+  std::string fatal;  // a driver failure fails every request after it
+  // statistics
+  std::vector<double> latencies;
+  int64_t completed = 0, failed = 0, iterations = 0;
+  std::chrono::steady_clock::time_point t_start = std::chrono::steady_clock::now(), t_last = t_start;
+};
+
+namespace {
+
+using SClock = std::chrono::steady_clock;
+double s_secs(SClock::time_point a, SClock::time_point b) { return std::chrono::duration<double>(b - a).count(); }
+
+void batch_driver(afp_batch_server* s) {
+  using namespace afp;
+  afp_amg* h = s->amg;
+  afp_context* ctx = h->ctx;
+  const int k = s->opts.width;
+  std::vector<afp_batch_server::Req*> slot(k, nullptr);
+  std::vector<int> iters(k, 0), act(k, 0);
+  std::vector<double> host(5 * MAXK);
+  try {
+    bind(ctx);
+    ensure_state(h, k);
+    MultiState& S = *h->multi;
+    const Level& L0 = h->lv[0];
+    const int64_t n = L0.n;
+    double* sc = S.scal.get();  // rows: 0 rz (old), 1 pq, 2 rr, 3 rz (new), 4 bb
+    double* partials = sc + 8 * MAXK;
+    const CSRView<double> A = L0.A<double>();
+    const unsigned rg = std::min<unsigned>(RED_GRID, rows_grid(ctx, n));
+    AFP_CUDA(cudaMemsetAsync(S.Rs.get(), 0, sizeof(double) * n * k, ctx->stream));
+    AFP_CUDA(cudaMemsetAsync(S.P.get(), 0, sizeof(double) * n * k, ctx->stream));
+    AFP_CUDA(cudaMemsetAsync(S.B.get(), 0, sizeof(double) * n * k, ctx->stream));
+    S.active.upload(act.data(), k);
+    sync(ctx);
+    for (;;) {
+      // ---- admission: queued requests into free columns
+      std::vector<std::pair<int, afp_batch_server::Req*>> admit;
+      {
+        std::unique_lock<std::mutex> lk(s->mu);
+        const bool any_active = std::find(act.begin(), act.end(), 1) != act.end();
+        if (!any_active) s->cv_work.wait(lk, [&] { return s->stop || !s->queue.empty(); });
+        if (s->stop && s->queue.empty() && !any_active) break;
+        for (int c = 0; c < k && !s->queue.empty(); ++c)
+          if (!act[c]) {
+            afp_batch_server::Req* r = s->queue.front();
+            s->queue.pop_front();
+            r->t_admit = SClock::now();
+            admit.push_back({c, r});
+          }
+      }
+      if (!admit.empty()) {
+        for (auto& [c, r] : admit) {
+          copy(ctx, S.Tmp.get() + (int64_t)c * n, r->b.data(), sizeof(double) * n);
+          k_col_admit<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, k, c, L0.perm.get(), S.Tmp.get() + (int64_t)c * n,
+                                                                S.B.get(), S.Xs.get(), S.Rs.get(), S.P.get());
+          check_launch(ctx, "batch admit");
+          slot[c] = r;
+          iters[c] = 0;
+          act[c] = 1;
+          host[c] = 1.0;  // old r.z of a fresh column
+        }
+        for (auto& [c, r] : admit) copy(ctx, sc + c, &host[c], sizeof(double));
+        S.active.upload(act.data(), k);
+        with_kpl(k, [&](auto KPLc) {
+          constexpr int KPL = decltype(KPLc)::value;
+          k_col_dot<KPL><<<rg, BLK, 0, ctx->stream>>>(n, S.B.get(), S.B.get(), k, partials, sc + 4 * MAXK);
+          check_launch(ctx, "batch b.b");
+        });
+      }
+      // ---- one CG iteration over every column (free ones are masked)
+      precondition_m(h);  // Z = V(R)
+      with_kpl(k, [&](auto KPLc) {
+        constexpr int KPL = decltype(KPLc)::value;
+        k_col_dot<KPL><<<rg, BLK, 0, ctx->stream>>>(n, S.Rs.get(), S.Z.get(), k, partials, sc + 3 * MAXK);
+        check_launch(ctx, "batch r.z");
+        k_update_p<KPL><<<rows_grid(ctx, n), BLK, 0, ctx->stream>>>(n, k, sc + 3 * MAXK, sc, S.active.get(),
+                                                                     S.Z.get(), S.P.get());
+        check_launch(ctx, "batch p");
+        k_spmm_dot<KPL><<<rg, BLK, 0, ctx->stream>>>(n, A.rowptr, A.cols, A.vals, S.P.get(), S.Q.get(), k, partials,
+                                                     sc + 1 * MAXK);
+        check_launch(ctx, "batch A p");
+        k_update_xr<KPL><<<rg, BLK, 0, ctx->stream>>>(n, k, sc + 3 * MAXK, sc + 1 * MAXK, S.active.get(), S.Xs.get(),
+                                                      S.Rs.get(), S.P.get(), S.Q.get(), partials, sc + 2 * MAXK);
+        check_launch(ctx, "batch x r");
+      });
+      AFP_CUDA(cudaMemcpyAsync(sc, sc + 3 * MAXK, sizeof(double) * k, cudaMemcpyDeviceToDevice, ctx->stream));
+      copy(ctx, host.data() + 2 * MAXK, sc + 2 * MAXK, sizeof(double) * 3 * MAXK);  // rr, rz, bb
+      sync(ctx);
+      // ---- retire converged (or failed) columns
+      std::vector<std::pair<int, int>> out;  // (column, status)
+      for (int c = 0; c < k; ++c) {
+        if (!act[c]) continue;
+        ++iters[c];
+        const double bn = std::max(std::sqrt(host[4 * MAXK + c]), 1e-300);
+        const double rel = std::sqrt(host[2 * MAXK + c]) / bn;
+        slot[c]->res.rel_residual = rel;
+        if (!std::isfinite(rel)) out.push_back({c, AFP_ERR_BREAKDOWN});
+        else if (rel <= s->opts.tol) out.push_back({c, AFP_OK});
+        else if (iters[c] >= s->opts.maxit) out.push_back({c, AFP_ERR_NOT_CONVERGED});
+      }
+      for (auto& [c, st] : out) {
+        afp_batch_server::Req* r = slot[c];
+        k_col_retire<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, k, c, L0.perm.get(), S.Xs.get(),
+                                                               S.Tmp.get() + (int64_t)c * n, S.Rs.get(), S.P.get());
+        check_launch(ctx, "batch retire");
+        r->x.resize(n);
+        copy(ctx, r->x.data(), S.Tmp.get() + (int64_t)c * n, sizeof(double) * n);
+        r->res.status = st;
+        r->res.iterations = iters[c];
+        act[c] = 0;
+      }
+      if (!out.empty()) {
+        S.active.upload(act.data(), k);
+        sync(ctx);
+        const auto now = SClock::now();
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto& [c, st] : out) {
+          afp_batch_server::Req* r = slot[c];
+          slot[c] = nullptr;
+          r->res.queue_seconds = s_secs(r->t_submit, r->t_admit);
+          r->res.latency_seconds = s_secs(r->t_submit, now);
+          r->done = true;
+          if (st == AFP_OK) {
+            s->completed++;
+            s->latencies.push_back(r->res.latency_seconds);
+          } else {
+            s->failed++;
+          }
+          s->t_last = now;
+        }
+        s->cv_done.notify_all();
+      }
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->iterations++;
+      }
+    }
+  } catch (const Error& e) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->fatal = e.msg;
+    for (auto& kv : s->reqs)
+      if (!kv.second->done) {
+        kv.second->res.status = e.status;
+        kv.second->done = true;
+        s->failed++;
+      }
+    s->queue.clear();
+    s->cv_done.notify_all();
+  }
+}
+
+double s_percentile(std::vector<double> v, double p) {
+  if (v.empty()) return 0.0;
+  std::sort(v.begin(), v.end());
+  const double pos = p / 100.0 * (v.size() - 1);
+  const size_t i = (size_t)pos;
+  const double frac = pos - i;
+  return i + 1 < v.size() ? v[i] * (1 - frac) + v[i + 1] * frac : v[i];
+}
+
+}  // namespace
+
+extern "C" {
+
+void afp_batch_default_opts(afp_batch_opts* o) {
+  if (!o) return;
+  o->width = 32;
+  o->tol = 1e-10;
+  o->maxit = 500;
+}
+
+afp_status afp_batch_server_create(afp_amg* amg, const afp_batch_opts* opts, afp_batch_server** out) {
+  return afp::guarded([&] {
+    AFP_REQUIRE(amg && out, AFP_ERR_INVALID, "null argument");
+    auto s = std::make_unique<afp_batch_server>();
+    if (opts) s->opts = *opts;
+    else afp_batch_default_opts(&s->opts);
+    AFP_REQUIRE(s->opts.width >= 1 && s->opts.width <= afp::MAXK, AFP_ERR_INVALID, "width must be in [1, 64]");
+    AFP_REQUIRE(s->opts.tol > 0 && s->opts.maxit >= 1, AFP_ERR_INVALID, "bad tolerance or iteration limit");
+    s->amg = amg;
+    s->driver = std::thread(batch_driver, s.get());
+    *out = s.release();
+  });
+}
+
+afp_status afp_batch_server_submit(afp_batch_server* s, const double* b, int64_t* ticket) {
+  return afp::guarded([&] {
+    AFP_REQUIRE(s && b && ticket, AFP_ERR_INVALID, "null argument");
+    const int64_t n = s->amg->lv[0].n;
+    auto r = std::make_unique<afp_batch_server::Req>();
+    r->b.assign(b, b + n);
+    r->t_submit = SClock::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    AFP_REQUIRE(!s->stop, AFP_ERR_INVALID, "server is shutting down");
+    AFP_REQUIRE(s->fatal.empty(), AFP_ERR_CUDA, "the server failed: " + s->fatal);
+    r->ticket = s->next_ticket++;
+    *ticket = r->ticket;
+    s->queue.push_back(r.get());
+    s->reqs[r->ticket] = std::move(r);
+    s->cv_work.notify_all();
+  });
+}
+
+afp_status afp_batch_server_wait(afp_batch_server* s, int64_t ticket, double* x, afp_request_result* res) {
+  return afp::guarded([&] {
+    AFP_REQUIRE(s, AFP_ERR_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    AFP_REQUIRE(it != s->reqs.end(), AFP_ERR_INVALID, "unknown ticket");
+    afp_batch_server::Req* r = it->second.get();
+    s->cv_done.wait(lk, [&] { return r->done; });
+    if (res) *res = r->res;
+    if (x && !r->x.empty()) std::memcpy(x, r->x.data(), sizeof(double) * r->x.size());
+    s->reqs.erase(it);
+  });
+}
+
+afp_status afp_batch_server_get_stats(afp_batch_server* s, afp_server_stats* st) {
+  return afp::guarded([&] {
+    AFP_REQUIRE(s && st, AFP_ERR_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    st->completed = s->completed;
+    st->failed = s->failed;
+    st->queued = (int64_t)s->queue.size();
+    st->p50_seconds = s_percentile(s->latencies, 50);
+    st->p99_seconds = s_percentile(s->latencies, 99);
+    const double span = s_secs(s->t_start, s->t_last);
+    st->solves_per_second = span > 0 ? s->completed / span : 0.0;
+    st->budget_bytes = 0;
+    st->in_use_bytes = 0;
+  });
+}
+
+afp_status afp_batch_server_reset_stats(afp_batch_server* s) {
+  return afp::guarded([&] {
+    AFP_REQUIRE(s, AFP_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->latencies.clear();
+    s->completed = s->failed = 0;
+    s->t_start = s->t_last = SClock::now();
+  });
+}
+
+afp_status afp_batch_server_destroy(afp_batch_server* s) {
+  return afp::guarded([&] {
+    if (!s) return;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->stop = true;
+    }
+    s->cv_work.notify_all();
+    if (s->driver.joinable()) s->driver.join();
+    delete s;
+  });
+}
+
+}  // extern "C"
+
+namespace afp {
+// Measurement of the batched V-cycle at the width of the last batched solve:
+// kind 4 = one batched V-cycle, kind 5 = one batched Gauss-Seidel sweep of
+// `level` (every colour class once); mean device time over reps and the
+// algorithmic bytes (each array once per pass, the k columns of a vector
+// block counted once per pass).
+void time_multi(afp_amg* h, int kind, int level, int reps, double* ms, double* bytes) {
+  AFP_REQUIRE(h->multi && h->multi->k > 0, AFP_ERR_INVALID, "no batched state: run a batched solve first");
+  afp_context* ctx = h->ctx;
+  MultiState& S = *h->multi;
+  const int k = S.k;
+  const bool mixed = S.mixed;
+  const double v = mixed ? 4.0 : 8.0, vp = mixed ? (h->opts.interp_bf16 ? 2.0 : 4.0) : 8.0;
+  auto unit = [&]() {
+    if (kind == 4) {
+      precondition_m(h);
+      return;
+    }
+    const Level& L = h->lv[level];
+    const int K = (int)L.cls.size() - 1;
+    for (int q = 0; q < K; ++q) {
+      const int64_t r0 = L.cls[q], r1 = L.cls[q + 1];
+      if (mixed) {
+        CSRView<float> A = L.A<float>();
+        if (L.overflow && q == K - 1) {
+          rows_m<float, float, RO_JAC>(ctx, r0, r1, A.rowptr, A.cols, A.vals, S.X32[level].get(), S.T32[level].get(),
+                                       S.R32[level].get(), L.l1d32.get(), k, "mrhs l1-jacobi");
+          k_copy<float><<<grid_for((r1 - r0) * k, BLK), BLK, 0, ctx->stream>>>((r1 - r0) * k, S.T32[level].get(),
+                                                                               S.X32[level].get() + r0 * k);
+          check_launch(ctx, "mrhs copy");
+        } else {
+          rows_m<float, float, RO_GS>(ctx, r0, r1, A.rowptr, A.cols, A.vals, S.X32[level].get(), S.X32[level].get(),
+                                      S.R32[level].get(), nullptr, k, "mrhs gauss-seidel class");
+        }
+      } else {
+        CSRView<double> A = L.A<double>();
+        if (L.overflow && q == K - 1) {
+          rows_m<double, double, RO_JAC>(ctx, r0, r1, A.rowptr, A.cols, A.vals, S.X[level].get(), S.T[level].get(),
+                                         S.R[level].get(), L.l1d.get(), k, "mrhs l1-jacobi");
+          k_copy<double><<<grid_for((r1 - r0) * k, BLK), BLK, 0, ctx->stream>>>((r1 - r0) * k, S.T[level].get(),
+                                                                                S.X[level].get() + r0 * k);
+          check_launch(ctx, "mrhs copy");
+        } else {
+          rows_m<double, double, RO_GS>(ctx, r0, r1, A.rowptr, A.cols, A.vals, S.X[level].get(), S.X[level].get(),
+                                        S.R[level].get(), nullptr, k, "mrhs gauss-seidel class");
+        }
+      }
+    }
+  };
+  AFP_REQUIRE(kind == 4 || (level >= 0 && level < h->t), AFP_ERR_INVALID, "level is not a smoothed level");
+  unit();  // warm
+  cudaEvent_t e0, e1;
+  AFP_CUDA(cudaEventCreate(&e0));
+  AFP_CUDA(cudaEventCreate(&e1));
+  AFP_CUDA(cudaEventRecord(e0, ctx->stream));
+  for (int i = 0; i < reps; ++i) unit();
+  AFP_CUDA(cudaEventRecord(e1, ctx->stream));
+  sync(ctx);
+  float t = 0;
+  AFP_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t / reps;
+  auto pass = [&](const Level& Q) { return (double)Q.nnz * (v + 4) + 4.0 * (Q.n + 1) + 3.0 * Q.n * v * k; };
+  if (kind == 5) {
+    *bytes = pass(h->lv[level]);
+    return;
+  }
+  const double s = h->opts.smooth_step;
+  double b = 0;
+  for (int l = 0; l < h->t; ++l) {
+    const Level& Q = h->lv[l];
+    const double nn = (double)Q.n, nc = (double)h->lv[l + 1].n;
+    b += (2 * s + 1) * pass(Q) + 2.0 * nn * v * k;                          // sweeps, residual, zero
+    b += 2.0 * Q.pnnz * (vp + 4) + 4.0 * (nc + 1) + 4.0 * (nn + 1) + 3.0 * nn * v * k + 2.0 * nc * v * k;  // P, P^T
+  }
+  const double nt = (double)h->lv[h->t].n;
+  b += h->tail_dense ? nt * nt * 8.0 + 2.0 * nt * v * k : 0.0;
+  *bytes = b;
+}
 }  // namespace afp

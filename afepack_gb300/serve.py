@@ -78,3 +78,62 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+class BatchServer:
+    """Continuous batching of right-hand sides against one resident hierarchy
+    (afp_batch_server_* in the C ABI): `width` CG columns stay in flight;
+    requests join free columns between CG iterations and leave when solved.
+
+        with BatchServer(amg, width=32) as srv:
+            t = srv.submit(b)            # numpy array, n doubles
+            x, result = srv.wait(t)
+    """
+
+    def __init__(self, amg, width: int = 32, tol: float = 1e-10, maxit: int = 500):
+        o = N.BatchOpts()
+        N.lib().afp_batch_default_opts(C.byref(o))
+        o.width, o.tol, o.maxit = width, tol, maxit
+        h = C.c_void_p()
+        N.call("afp_batch_server_create", amg.handle, C.byref(o), C.byref(h))
+        self.handle = h
+        self.amg = amg  # keeps the hierarchy alive
+        self.n = amg.level_info(0)[0]
+
+    def submit(self, b) -> int:
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        assert b.shape == (self.n,)
+        t = C.c_int64()
+        N.call("afp_batch_server_submit", self.handle, b.ctypes.data, C.byref(t))
+        return t.value
+
+    def wait(self, ticket: int):
+        x = np.empty(self.n)
+        res = N.RequestResult()
+        N.call("afp_batch_server_wait", self.handle, ticket, x.ctypes.data, C.byref(res))
+        return x, res.as_dict()
+
+    def stats(self):
+        s = N.ServerStats()
+        N.call("afp_batch_server_get_stats", self.handle, C.byref(s))
+        return s.as_dict()
+
+    def reset_stats(self):
+        N.call("afp_batch_server_reset_stats", self.handle)
+
+    def close(self):
+        if self.handle:
+            N.lib().afp_batch_server_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -6,15 +6,20 @@ Workload (default): 3D Poisson, P1 on a 64^3 Kuhn-split unit cube
 Gaussians, zero Dirichlet data, b = M f.  Seeded synthetic input; no public
 data set is involved.
 
-A step is one solve request against the device-resident operator and AMG
-hierarchy: CG preconditioned by one V-cycle per iteration until
-||b - A x||_2 <= tol ||b||_2, from x = 0.  `value` is mixed-precision solves/s
-(FP32 V-cycle with a double-float dense tail, FP64 CG recurrences) at tol
-1e-10, whose
-error against the FP64 reference solution is reported; the plain FP64 GPU
-drop-in's solves/s is reported beside it.  Assembly, Dirichlet elimination
-and AMG setup are timed once and reported (`setup`), as are the whole
-request latencies.  L2 is flushed (a 512 MB write) before every timed step.
+The operator and its AMG hierarchy are set up once and stay resident.  A
+step is one batched solve of `--width` (64) requests -- right-hand sides
+b_j = M f_j, f_j a sum of 8 Gaussians drawn per request like the workload's
+f -- by CG preconditioned with one mixed-precision V-cycle per iteration
+(FP32 V-cycle with a double-float dense tail, FP64 CG recurrences) to
+||b - A x||_2 <= tol ||b||_2 (1e-10) per request.  `value` is those solves/s
+with the inputs resident on the device; `e2e` is the same requests served
+through the C ABI batch server (afp_batch_server_*: continuous batching,
+requests join free columns between CG iterations) with host buffers in and
+out, all submitted at once; `served` adds Poisson arrivals at 60% of that
+rate with p50/p99 latency.  Beside them: the plain FP64 GPU drop-in
+(`fp64`, one solve at a time) and single mixed solves (`mixed_single`).
+Assembly, Dirichlet elimination and AMG setup are timed once (`setup`).  L2
+is flushed (a 512 MB write) before every timed step.
 
     python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -50,6 +55,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="poisson3d_p1_64", choices=sorted(WORKLOADS))
     ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--width", type=int, default=64, help="requests per batched step / batch-server columns")
+    ap.add_argument("--served", type=int, default=256, help="requests sent through the batch server")
     ap.add_argument("--stream", action="store_true", help="served request stream instead of one workload")
     ap.add_argument("--stream-sample", type=int, default=48)
     ap.add_argument("--workers", type=int, default=8)
@@ -257,8 +264,6 @@ def run_ours(args):
         for _ in range(max(args.warmup, 3)):
             solve(amg, args.tol)
         times, iters = [], []
-        if name == "mixed":
-            clocks.start()
         # named range of the timed solves ("timed_fp64" / "timed_mixed"), so a
         # profiler's launch list can be limited to them (ncu --nvtx-include)
         torch.cuda.synchronize()
@@ -276,34 +281,94 @@ def run_ours(args):
             iters.append(info["iterations"])
         torch.cuda.nvtx.range_pop()
         barrier()
-        if name == "mixed":
-            clk = clocks.stop()
         err = float(torch.linalg.norm(x - x_ref) / torch.linalg.norm(x_ref))
         t = np.array(times)
         results[name] = {"solves_per_s": 1e3 * len(t) / t.sum(), "ms_mean": float(t.mean()),
                          "p50_ms": float(np.percentile(t, 50)), "p99_ms": float(np.percentile(t, 99)),
                          "pcg_iterations": int(np.median(iters)), "rel_err_vs_fp64": err}
 
-    phase("timed solves")
-    # ---- end to end through the C ABI with host buffers (H2D of b, D2H of x inside)
-    b_host = b.cpu().numpy().copy()
-    bh = torch.from_numpy(b_host).pin_memory()
-    xh = torch.zeros(bh.shape[0], dtype=torch.float64).pin_memory()
-    e2e_t = []
-    for i in range(args.warmup + args.steps):
+    phase("timed single solves")
+    # ---- served: many right-hand sides against the resident hierarchy.
+    # Requests: f_j drawn like the workload's f (sums of 8 Gaussians), b_j = M f_j
+    # with the Dirichlet rows zeroed (zero boundary data).
+    from afepack_gb300.serve import BatchServer
+    Wd = args.width
+    nreq_dev = Wd * (max(args.warmup, 3) + args.steps)
+    F = W.gaussian_sources(wl.space, nreq_dev + args.served, seed=5)
+    dmask = torch.from_numpy((wl.space.dof_bmark != 0)).to(dev)
+    Bcols = []
+    for j in range(F.shape[1]):
+        bj = M.vmult(torch.from_numpy(np.ascontiguousarray(F[:, j])).to(dev))
+        bj[dmask] = 0.0
+        Bcols.append(bj)
+    blocks = [torch.stack(Bcols[i * Wd:(i + 1) * Wd], dim=1).contiguous() for i in range(nreq_dev // Wd)]
+    served_b = [c.cpu().numpy() for c in Bcols[nreq_dev:]]
+    del Bcols
+    phase("request generation")
+    # device-resident batches (value): one step = one batched solve of Wd requests
+    for i in range(max(args.warmup, 3)):
+        amg32.pcg_multi(blocks[i], args.tol, 1000)
+    bt, bit = [], []
+    clocks.start()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.nvtx.range_push("timed_batched")
+    for i in range(args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
-        xh.zero_()
         s0, s1 = ev(), ev()
         s0.record(stream)
-        amg32.pcg(bh.numpy(), args.tol, 1000, xh.numpy())
+        Xb, infos = amg32.pcg_multi(blocks[max(args.warmup, 3) + i], args.tol, 1000)
         s1.record(stream)
         torch.cuda.synchronize()
-        if i >= args.warmup:
-            e2e_t.append(s0.elapsed_time(s1))
-    e2e_t = np.array(e2e_t)
-
-    phase("e2e")
+        bt.append(s0.elapsed_time(s1))
+        bit.append(max(inf["iterations"] for inf in infos))
+    torch.cuda.nvtx.range_pop()
+    barrier()
+    clk = clocks.stop()
+    bt = np.array(bt)
+    # error of a served (batched) solution against the FP64 GPU solve to 1e-14
+    j_last = blocks[-1][:, 0].contiguous()
+    xr_last, _ = amg64.pcg(j_last, 1e-14, 1000)
+    err_b = float(torch.linalg.norm(Xb[:, 0] - xr_last) / torch.linalg.norm(xr_last))
+    phase("timed batched solves")
+    # end to end through the C ABI batch server with host buffers: saturation
+    # (every request submitted at once), then Poisson arrivals at 60% of it
+    served = {}
+    with BatchServer(amg32, width=Wd, tol=args.tol, maxit=1000) as srv:
+        for t in [srv.submit(v) for v in served_b[:Wd]]:
+            srv.wait(t)
+        srv.reset_stats()
+        t0 = time.perf_counter()
+        tickets = [srv.submit(v) for v in served_b]
+        res = [srv.wait(t)[1] for t in tickets]
+        wall = time.perf_counter() - t0
+        lat = np.array([r["latency_seconds"] for r in res])
+        sat = len(res) / wall
+        served["saturation"] = {"requests": len(res), "solves_per_s": round(sat, 2),
+                                "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
+                                "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2),
+                                "failed": int(sum(r["status"] != 0 for r in res))}
+        rate = 0.6 * sat
+        gaps = np.random.default_rng(7).exponential(1.0 / rate, len(served_b))
+        srv.reset_stats()
+        t0 = time.perf_counter()
+        due = t0
+        tickets = []
+        for v, g in zip(served_b, gaps):
+            due += g
+            while time.perf_counter() < due:
+                time.sleep(0.0002)
+            tickets.append(srv.submit(v))
+        res = [srv.wait(t)[1] for t in tickets]
+        wall = time.perf_counter() - t0
+        lat = np.array([r["latency_seconds"] for r in res])
+        served["poisson_60pct"] = {"requests": len(res), "arrival_rate_per_s": round(rate, 2),
+                                   "solves_per_s": round(len(res) / wall, 2),
+                                   "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
+                                   "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2),
+                                   "failed": int(sum(r["status"] != 0 for r in res))}
+    phase("served through the batch server")
     # ---- roofline: kernels timed live with CUDA events on the library stream
     peaks = {}
     try:
@@ -313,30 +378,26 @@ def run_ours(args):
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     n0, nnz0, _ = levels[0]
     kernels = {}
-    units = [("vcycle_mixed", amg32, 2, 0), ("residual_level0_mixed", amg32, 1, 0)]
+    amg32.pcg_multi(blocks[0], args.tol, 1000)  # the batched state at width Wd
+    units = [("batched_vcycle_mixed", amg32, 4, 0)]
+    units += [(f"batched_gs_sweep_level{l}_mixed", amg32, 5, l) for l in range(len(levels) - 1)]
+    units += [("vcycle_mixed", amg32, 2, 0), ("residual_level0_mixed", amg32, 1, 0)]
     units += [(f"gs_sweep_level{l}_mixed", amg32, 0, l) for l in range(len(levels) - 1)]
     units += [("vcycle_fp64", amg64, 2, 0), ("gs_sweep_level0_fp64", amg64, 0, 0), ("spmv_fine_fp64", amg64, 3, 0)]
-    reps = 20
+    reps = 10
     for label, amg, kind, lev in units:
         c0 = ctx.launch_count()
         ms, nbytes = amg.time_kernel(kind, lev, reps)
         per_unit = (ctx.launch_count() - c0) / (reps + 1)  # the timer runs one warm-up unit first
         kernels[label] = {"ms": round(ms, 5), "bytes": int(nbytes), "GBps": round(nbytes / ms / 1e6, 1),
                           "frac": round(nbytes / ms / 1e6 / hbm, 4), "launches": round(per_unit, 2)}
-    if kernels["vcycle_mixed"]["launches"] <= 1.5:
-        # the V-cycle is one persistent kernel: it is the dominant kernel
-        dom = kernels["vcycle_mixed"]
-        name = ("k_vcycle_stream: one FP32 V-cycle (every level's Gauss-Seidel classes, residual, restriction, "
-                "dense double-float tail, prolongation) in one persistent launch")
-        ratio = profiled_ratio(args.workload, "vcycle_stream")
-    else:
-        # the Gauss-Seidel sweep of the level that takes longest (levels 1-2 of
-        # the 3D hierarchies: the largest share of the ncu launch list)
-        lev = max(range(len(levels) - 1), key=lambda l: kernels[f"gs_sweep_level{l}_mixed"]["ms"])
-        dom = kernels[f"gs_sweep_level{lev}_mixed"]
-        name = (f"k_gs_class<float> (+ k_jacobi_l1 overflow class): one Gauss-Seidel sweep of level {lev} "
-                f"({levels[lev][0]} rows, {dom['launches']:.0f} launches)")
-        ratio = profiled_ratio(args.workload, "gs_class_f32_vec32")
+    # the dominant kernel of the served path: the batched Gauss-Seidel sweep
+    # of the level that takes longest (k_rows_m, one launch per colour class)
+    lev = max(range(len(levels) - 1), key=lambda l: kernels[f"batched_gs_sweep_level{l}_mixed"]["ms"])
+    dom = kernels[f"batched_gs_sweep_level{lev}_mixed"]
+    name = (f"k_rows_m<float> Gauss-Seidel classes (+ l1-Jacobi overflow class): one batched sweep of level {lev} "
+            f"({levels[lev][0]} rows x {Wd} right-hand sides, {dom['launches']:.0f} launches)")
+    ratio = profiled_ratio(args.workload, "rows_m_gs_batched")
     traffic = int(ratio * dom["bytes"]) if ratio else None
     roof = {"bound": "hbm", "kernel": name, "achieved": dom["GBps"], "peak": hbm, "unit": "GB/s",
             "frac": dom["frac"], "traffic": traffic,
@@ -349,21 +410,28 @@ def run_ours(args):
     cpu = (cpu_baseline_sample(amg64, b.cpu().numpy().copy(), args.tol, results["fp64"]["pcg_iterations"])
            if world_size() == 1 else None)
     phase("CPU sample")
+    nb = int(blocks[0].shape[0])
     line = {
-        "metric": METRIC, "value": round(results["mixed"]["solves_per_s"], 3), "unit": "solves/s",
+        "metric": METRIC, "value": round(Wd * 1e3 * len(bt) / bt.sum(), 3), "unit": "solves/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(results["mixed"]["ms_mean"], 3), "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": round(float(bt.mean()), 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 V-cycle + fp64 CG", "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "n_dof": int(n0), "nnz": int(nnz0), "tol": args.tol,
-                   "levels": [list(map(int, l)) for l in levels], "l2": "flushed before every step (512 MB write)",
-                   "parallelism": "replicas only"},
-        "p50_ms": round(results["mixed"]["p50_ms"], 3), "p99_ms": round(results["mixed"]["p99_ms"], 3),
-        "rel_err_vs_fp64": results["mixed"]["rel_err_vs_fp64"], "fp64": results["fp64"],
-        "mixed_over_fp64": round(results["mixed"]["solves_per_s"] / results["fp64"]["solves_per_s"], 3),
+                   "requests_per_step": Wd, "levels": [list(map(int, l)) for l in levels],
+                   "step": f"one batched CG solve of {Wd} requests (different right-hand sides) against the resident "
+                           f"operator and hierarchy, inputs resident on the device",
+                   "l2": "flushed before every step (512 MB write)", "parallelism": "replicas only"},
+        "p50_ms": served["poisson_60pct"]["p50_ms"], "p99_ms": served["poisson_60pct"]["p99_ms"],
+        "served": served, "rel_err_vs_fp64": err_b, "pcg_iterations_max": int(max(bit)),
+        "fp64": results["fp64"], "mixed_single": results["mixed"],
+        "mixed_over_fp64": round(Wd * 1e3 * len(bt) / bt.sum() / results["fp64"]["solves_per_s"], 3),
+        "served_over_fp64": round(served["saturation"]["solves_per_s"] / results["fp64"]["solves_per_s"], 3),
         "setup": {k: round(v, 3) for k, v in setup.items()},
-        "e2e": {"value": round(1e3 * len(e2e_t) / e2e_t.sum(), 3), "unit": "solves/s",
-                "h2d_bytes_per_step": int(bh.numel() * 8), "d2h_bytes_per_step": int(xh.numel() * 8),
-                "p50_ms": round(float(np.percentile(e2e_t, 50)), 3), "p99_ms": round(float(np.percentile(e2e_t, 99)), 3)},
+        "e2e": {"value": served["saturation"]["solves_per_s"], "unit": "solves/s",
+                "h2d_bytes_per_step": int(Wd * nb * 8), "d2h_bytes_per_step": int(Wd * nb * 8),
+                "p50_ms": served["saturation"]["p50_ms"], "p99_ms": served["saturation"]["p99_ms"],
+                "how": f"the batch server through the C ABI (afp_batch_server_*), {Wd} columns, host buffers in and out, "
+                       f"{served['saturation']['requests']} requests submitted at once; a step = {Wd} requests"},
         "roofline": roof, "clocks": clk, "gpu_launches": int(launches), "cpu_baseline": cpu,
     }
     return line

@@ -235,7 +235,9 @@ afp_status afp_amg_download_projection(const afp_amg *amg, int level, int32_t *r
  * on the context's stream) and its algorithmic bytes (compulsory traffic:
  * each array once per pass).  kind: 0 = one Gauss-Seidel sweep over all
  * colour classes of `level`, 1 = the residual SpMV of `level`, 2 = one
- * V-cycle, 3 = the FP64 fine-level SpMV of the CG.  The precision is the
+ * V-cycle, 3 = the FP64 fine-level SpMV of the CG; at the width of the last
+ * batched solve (afp_pcg_solve_multi or a batch server), 4 = one batched
+ * V-cycle and 5 = one batched sweep of `level`.  The precision is the
  * solver's. */
 afp_status afp_amg_time_kernel(afp_amg *amg, int kind, int level, int reps, double *ms, double *bytes);
 
@@ -324,6 +326,33 @@ afp_status afp_server_get_stats(afp_server *s, afp_server_stats *stats);
 afp_status afp_server_reset_stats(afp_server *s);
 /* Finishes queued requests, then stops the slots. */
 afp_status afp_server_destroy(afp_server *s);
+
+/* A batching server for many right-hand sides against one resident
+ * hierarchy (no counterpart in the reference): requests carry only b; the
+ * server keeps `width` CG columns of the hierarchy's batched solver in flight
+ * and, between two CG iterations, admits queued requests into free columns
+ * and returns the ones that reached tol, so requests join and leave while
+ * others are being solved (every iteration is one batched V-cycle over all
+ * columns).  A request's solution does not depend on the other columns.
+ * While a server exists, the hierarchy must not be used by other calls. */
+typedef struct afp_batch_server afp_batch_server;
+
+typedef struct afp_batch_opts {
+  int width;                   /* columns (execution slots), 1..64 (default 32) */
+  double tol;                  /* relative residual of each CG (default 1e-10) */
+  int maxit;                   /* CG iteration limit (default 500)             */
+} afp_batch_opts;
+
+void afp_batch_default_opts(afp_batch_opts *opts);
+afp_status afp_batch_server_create(afp_amg *amg, const afp_batch_opts *opts, afp_batch_server **out);
+/* b: host array of n doubles (reference order), copied before returning. */
+afp_status afp_batch_server_submit(afp_batch_server *s, const double *b, int64_t *ticket);
+/* Blocks until the request is done; x (n doubles) receives its solution. */
+afp_status afp_batch_server_wait(afp_batch_server *s, int64_t ticket, double *x, afp_request_result *res);
+afp_status afp_batch_server_get_stats(afp_batch_server *s, afp_server_stats *stats);
+afp_status afp_batch_server_reset_stats(afp_batch_server *s);
+/* Finishes queued and running requests, then stops. */
+afp_status afp_batch_server_destroy(afp_batch_server *s);
 
 /* ----------------------------------------------------------- host logic */
 /* The C/F splitting and projection of one level (Project, src/AMGSolver.cpp:18-226),

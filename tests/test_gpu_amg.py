@@ -346,3 +346,39 @@ def test_server_admission_by_memory(ctx):
         ts = [srv.submit(wl) for wl in reqs]
         out = [srv.wait(t) for t in ts]
     assert all(r["status"] == 0 for _, r in out)
+
+
+def test_batch_server_results_same_alone_and_in_the_mix(ctx):
+    """Continuous batching against one resident hierarchy: requests submitted
+    while others are in flight join free columns between CG iterations; each
+    served solution equals (to the CG tolerance) the same request served alone,
+    and the FP64 direct solution to 1e-8."""
+    import time
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import MIXED, AMGSolver
+    from afepack_gb300.serve import BatchServer
+    wl = W.poisson2d_p1(96)
+    _, K, b = system(ctx, wl)
+    amg = AMGSolver(K, precision=MIXED)
+    rng = np.random.default_rng(12)
+    interior = wl.space.dof_bmark == 0
+    rhs = [b * (1 + 0.3 * rng.standard_normal()) + 1e-3 * rng.standard_normal(b.shape) * interior for _ in range(11)]
+    with BatchServer(amg, width=4, tol=1e-10) as alone:
+        solo = [alone.wait(alone.submit(v)) for v in rhs[:3]]
+    with BatchServer(amg, width=4, tol=1e-10) as srv:
+        tickets = []
+        for i, v in enumerate(rhs):  # staggered: some arrive while others run
+            tickets.append(srv.submit(v))
+            if i % 3 == 2:
+                time.sleep(0.002)
+        out = [srv.wait(t) for t in tickets]
+        st = srv.stats()
+    assert st["completed"] == len(rhs) and st["failed"] == 0
+    assert max(r["queue_seconds"] for _, r in out) > 0  # more requests than columns: some queued
+    for (xs, rs), (xm, rm) in zip(solo, out[:3]):
+        assert rs["status"] == 0 and rm["status"] == 0
+        assert np.linalg.norm(xm - xs) <= 1e-9 * np.linalg.norm(xs)
+    for v, (x, r) in zip(rhs, out):
+        assert r["rel_residual"] <= 1e-10
+        xd = direct(K, v)
+        assert np.linalg.norm(x - xd) <= 1e-8 * np.linalg.norm(xd)
