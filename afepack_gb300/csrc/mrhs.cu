@@ -84,61 +84,99 @@ __global__ void k_dense_gemm(int64_t n, const X* __restrict__ M, const X* __rest
 
 // --------------------------------------------------- V-cycle row kernels
 // One kernel for every row operation of the batched V-cycle on rows [r0, r1)
-// of an n x k block: a sub-warp of W lanes (a power of two, W >= k up to 32)
-// takes one row, lane l owning columns l, l + W, ... (KPL of them).  The
-// row's (column, value) pairs are loaded W at a time, one per lane, and
-// broadcast with shuffles; the gathers of x rows they address are issued four
-// entries ahead (unrolled), so a row costs about two dependent memory round
-// trips whatever its length.
+// of an n x k block.  A group of W lanes (a power of two, W >= k up to 32)
+// holds the row's k columns, lane l owning columns l, l + W, ... (KPL of
+// them); SPL groups share one row, group p taking the row's entries in chunks
+// p, p + SPL, ... of W (long coarse-level rows: enough groups in flight to
+// cover the gather latency).  A chunk's (column, value) pairs are loaded one
+// per lane and broadcast with shuffles; the gathers of the x rows of U = 8
+// entries are issued before any of their products is summed.  The groups'
+// partial sums meet in shared memory and are added in group order, so the
+// result does not depend on timing.
 enum RowOp { RO_SPMM = 0, RO_SPMM_ADD, RO_RES, RO_GS, RO_JAC };
 
-template <int W, int KPL, class V, class X, int OP>
-__global__ void k_rows_m(int64_t r0, int64_t r1, const int* __restrict__ rp, const int* __restrict__ ci,
-                         const V* __restrict__ va, const X* x, X* y, const X* __restrict__ r,
-                         const X* __restrict__ d, int k) {
+constexpr int ROWS_BLK = 256;
+
+template <int W, int KPL, int SPL, class V, class X, int OP>
+__global__ void __launch_bounds__(ROWS_BLK) k_rows_m(int64_t r0, int64_t r1, const int* __restrict__ rp,
+                                                     const int* __restrict__ ci, const V* __restrict__ va, const X* x,
+                                                     X* y, const X* __restrict__ r, const X* __restrict__ d, int k) {
   using A = typename AccT<X>::type;
-  const int64_t row = r0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / W;
-  if (row >= r1) return;  // a whole sub-warp leaves together
-  const int lane = threadIdx.x & (W - 1);
+  constexpr int GPB = ROWS_BLK / W;  // groups per block
+  __shared__ A part[SPL > 1 ? GPB : 1][SPL > 1 ? W : 1][KPL];
+  const int grp = threadIdx.x / W, lane = threadIdx.x & (W - 1);
+  const int64_t row = r0 + (int64_t)blockIdx.x * (GPB / SPL) + grp / SPL;
+  const int pidx = grp % SPL;
+  const bool on = row < r1;
   const unsigned mask = W >= 32 ? 0xffffffffu : (((1u << W) - 1u) << ((threadIdx.x & 31) & ~(W - 1)));
   A acc[KPL];
 #pragma unroll
   for (int q = 0; q < KPL; ++q) acc[q] = 0;
-  int b = rp[row];
-  const int e = rp[row + 1];
   A diag = 1;
-  if (OP == RO_GS) {  // the diagonal is the row's first entry
-    diag = as<A>(va[b]);
-    ++b;
-  }
-  if (W == 1) {
-#pragma unroll 4
-    for (int j = b; j < e; ++j) {
-      const A val = as<A>(va[j]);
-      const X* xr = x + (int64_t)ci[j] * k;
-#pragma unroll
-      for (int q = 0; q < KPL; ++q)
-        if (q < k) acc[q] += val * (A)xr[q];
+  if (on) {
+    int b = rp[row];
+    const int e = rp[row + 1];
+    if (OP == RO_GS) {  // the diagonal is the row's first entry
+      diag = as<A>(va[b]);
+      ++b;
     }
-  } else {
-    for (int base = b; base < e; base += W) {
-      const int my = base + lane;
-      const int cc = my < e ? ci[my] : 0;
-      const A vv = my < e ? as<A>(va[my]) : A(0);
-      const int cnt = min(W, e - base);
-#pragma unroll 4
-      for (int jj = 0; jj < cnt; ++jj) {
-        const int col = __shfl_sync(mask, cc, jj, W);
-        const A val = __shfl_sync(mask, vv, jj, W);
-        const X* xr = x + (int64_t)col * k;
+    constexpr int U = 8;
+    if (W == 1) {
+      for (int j0 = b + pidx * U; j0 < e; j0 += SPL * U) {
+        A vals[U];
+        X xv[U];
 #pragma unroll
-        for (int q = 0; q < KPL; ++q) {
-          const int c = lane + W * q;
-          if (c < k) acc[q] += val * (A)xr[c];
+        for (int u = 0; u < U; ++u) {
+          const bool in = j0 + u < e;
+          vals[u] = in ? as<A>(va[j0 + u]) : A(0);
+          xv[u] = in ? x[(int64_t)ci[j0 + u] * k] : X(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc[0] += vals[u] * (A)xv[u];
+      }
+    } else {
+      for (int base = b + pidx * W; base < e; base += SPL * W) {
+        const int my = base + lane;
+        const int cc = my < e ? ci[my] : 0;
+        const A vv = my < e ? as<A>(va[my]) : A(0);
+        const int cnt = min(W, e - base);
+        for (int jj = 0; jj < cnt; jj += U) {
+          A vals[U];
+          X xv[U][KPL];
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const bool in = jj + u < cnt;  // the same for the whole group
+            const int col = __shfl_sync(mask, cc, in ? jj + u : 0, W);
+            const A val = __shfl_sync(mask, vv, in ? jj + u : 0, W);
+            vals[u] = in ? val : A(0);
+            const X* xr = x + (int64_t)col * k;
+#pragma unroll
+            for (int q = 0; q < KPL; ++q) {
+              const int c = lane + W * q;
+              xv[u][q] = (in && c < k) ? xr[c] : X(0);
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int q = 0; q < KPL; ++q) acc[q] += vals[u] * (A)xv[u][q];
         }
       }
     }
   }
+  if (SPL > 1) {
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) part[grp][lane][q] = acc[q];
+    __syncthreads();
+    if (pidx != 0) return;
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) {
+      A s = part[grp][lane][q];
+      for (int p = 1; p < SPL; ++p) s += part[grp + p][lane][q];
+      acc[q] = s;
+    }
+  }
+  if (!on) return;
 #pragma unroll
   for (int q = 0; q < KPL; ++q) {
     const int c = lane + W * q;
@@ -152,16 +190,28 @@ __global__ void k_rows_m(int64_t r0, int64_t r1, const int* __restrict__ rp, con
   }
 }
 
-// Launches k_rows_m with W = the smallest power of two >= k (at most 32) and
-// KPL = columns per lane.
+// Launches k_rows_m with W = the smallest power of two >= k (at most 32),
+// KPL = columns per lane, and SPL groups per row for rows of about
+// `row_len` entries (about 48 entries per group).
 template <class V, class X, int OP>
 void rows_m(const afp_context* ctx, int64_t r0, int64_t r1, const int* rp, const int* ci, const V* va, const X* x,
-            X* y, const X* r, const X* d, int k, const char* what) {
+            X* y, const X* r, const X* d, int k, double row_len, const char* what) {
   if (r1 <= r0) return;
+  int spl = 1;
+  while (spl < 8 && spl * 48 < row_len) spl *= 2;
   auto go = [&](auto Wc, auto Kc) {
     constexpr int W = decltype(Wc)::value, KPL = decltype(Kc)::value;
-    k_rows_m<W, KPL, V, X, OP><<<grid_for((r1 - r0) * W, 256), 256, 0, ctx->stream>>>(r0, r1, rp, ci, va, x, y, r, d,
-                                                                                     k);
+    auto launch = [&](auto Sc) {
+      constexpr int SPL = decltype(Sc)::value;
+      constexpr int rows_per_blk = ROWS_BLK / W / SPL > 0 ? ROWS_BLK / W / SPL : 1;
+      static_assert(ROWS_BLK / W >= SPL, "a block holds whole rows");
+      const unsigned grid = (unsigned)((r1 - r0 + rows_per_blk - 1) / rows_per_blk);
+      k_rows_m<W, KPL, SPL, V, X, OP><<<grid, ROWS_BLK, 0, ctx->stream>>>(r0, r1, rp, ci, va, x, y, r, d, k);
+    };
+    if (spl == 1) launch(std::integral_constant<int, 1>());
+    else if (spl == 2) launch(std::integral_constant<int, 2>());
+    else if (spl == 4) launch(std::integral_constant<int, 4>());
+    else launch(std::integral_constant<int, 8>());
   };
   using I1 = std::integral_constant<int, 1>;
   using I2 = std::integral_constant<int, 2>;
@@ -442,6 +492,7 @@ void vcycle_m(afp_amg* h, MultiState& S) {
   auto smooth = [&](int l, X* x, const X* r, bool backward) {
     const Level& L = h->lv[l];
     CSRView<X> A = L.A<X>();
+    const double len = (double)L.nnz / (double)L.n;
     const int K = (int)L.cls.size() - 1;
     for (int s = 0; s < h->opts.smooth_step; ++s)
       for (int q = 0; q < K; ++q) {
@@ -453,11 +504,12 @@ void vcycle_m(afp_amg* h, MultiState& S) {
           if constexpr (std::is_same<X, double>::value) d = L.l1d.get();
           else d = L.l1d32.get();
           X* tmp = blk<X>(S, 2, l);
-          rows_m<X, X, RO_JAC>(ctx, r0, r1, A.rowptr, A.cols, A.vals, x, tmp, r, d, k, "mrhs l1-jacobi");
+          rows_m<X, X, RO_JAC>(ctx, r0, r1, A.rowptr, A.cols, A.vals, x, tmp, r, d, k, len, "mrhs l1-jacobi");
           k_copy<X><<<grid_for((r1 - r0) * k, BLK), BLK, 0, ctx->stream>>>((r1 - r0) * k, tmp, x + r0 * k);
           check_launch(ctx, "mrhs copy");
         } else {
-          rows_m<X, X, RO_GS>(ctx, r0, r1, A.rowptr, A.cols, A.vals, x, x, r, nullptr, k, "mrhs gauss-seidel class");
+          rows_m<X, X, RO_GS>(ctx, r0, r1, A.rowptr, A.cols, A.vals, x, x, r, nullptr, k, len,
+                              "mrhs gauss-seidel class");
         }
       }
   };
@@ -469,10 +521,11 @@ void vcycle_m(afp_amg* h, MultiState& S) {
     check_launch(ctx, "mrhs zero");
     smooth(l, x, r, false);
     CSRView<X> A = L.A<X>();
-    rows_m<X, X, RO_RES>(ctx, 0, L.n, A.rowptr, A.cols, A.vals, x, blk<X>(S, 2, l), r, nullptr, k, "mrhs residual");
+    rows_m<X, X, RO_RES>(ctx, 0, L.n, A.rowptr, A.cols, A.vals, x, blk<X>(S, 2, l), r, nullptr, k,
+                         (double)L.nnz / L.n, "mrhs residual");
     const int64_t nc = h->lv[l + 1].n;
     rows_m<PV, X, RO_SPMM>(ctx, 0, nc, L.prp.get(), L.pci.get(), p_vals<PV>(L), blk<X>(S, 2, l), blk<X>(S, 1, l + 1),
-                           nullptr, nullptr, k, "mrhs restriction");
+                           nullptr, nullptr, k, (double)L.pnnz / nc, "mrhs restriction");
   }
   const Level& T = h->lv[t];
   if (h->tail_dense) {
@@ -497,7 +550,7 @@ void vcycle_m(afp_amg* h, MultiState& S) {
   for (int l = t - 1; l >= 0; --l) {
     Level& L = h->lv[l];
     rows_m<PV, X, RO_SPMM_ADD>(ctx, 0, L.n, L.trp.get(), L.tci.get(), pt_vals<PV>(L), blk<X>(S, 0, l + 1),
-                               blk<X>(S, 0, l), nullptr, nullptr, k, "mrhs prolongation");
+                               blk<X>(S, 0, l), nullptr, nullptr, k, (double)L.pnnz / L.n, "mrhs prolongation");
     smooth(l, blk<X>(S, 0, l), blk<X>(S, 1, l), h->opts.symmetric != 0);
   }
 }
@@ -613,7 +666,7 @@ bool pcg_multi(afp_amg* h, double* X_user, const double* B_user, int nrhs, doubl
   const CSRView<double> A = L0.A<double>();
   const unsigned rg = std::min<unsigned>(RED_GRID, rows_grid(ctx, n));
   rows_m<double, double, RO_RES>(ctx, 0, n, A.rowptr, A.cols, A.vals, S.Xs.get(), S.Rs.get(), S.B.get(), nullptr, k,
-                                 "mrhs residual");
+                                 (double)L0.nnz / n, "mrhs residual");
   with_kpl(k, [&](auto KPLc) {
     constexpr int KPL = decltype(KPLc)::value;
     k_col_dot<KPL><<<rg, BLK, 0, ctx->stream>>>(n, S.B.get(), S.B.get(), k, partials, sc + 4 * MAXK);
@@ -1047,6 +1100,7 @@ void time_multi(afp_amg* h, int kind, int level, int reps, double* ms, double* b
       return;
     }
     const Level& L = h->lv[level];
+    const double len = (double)L.nnz / (double)L.n;
     const int K = (int)L.cls.size() - 1;
     for (int q = 0; q < K; ++q) {
       const int64_t r0 = L.cls[q], r1 = L.cls[q + 1];
@@ -1054,25 +1108,25 @@ void time_multi(afp_amg* h, int kind, int level, int reps, double* ms, double* b
         CSRView<float> A = L.A<float>();
         if (L.overflow && q == K - 1) {
           rows_m<float, float, RO_JAC>(ctx, r0, r1, A.rowptr, A.cols, A.vals, S.X32[level].get(), S.T32[level].get(),
-                                       S.R32[level].get(), L.l1d32.get(), k, "mrhs l1-jacobi");
+                                       S.R32[level].get(), L.l1d32.get(), k, len, "mrhs l1-jacobi");
           k_copy<float><<<grid_for((r1 - r0) * k, BLK), BLK, 0, ctx->stream>>>((r1 - r0) * k, S.T32[level].get(),
                                                                                S.X32[level].get() + r0 * k);
           check_launch(ctx, "mrhs copy");
         } else {
           rows_m<float, float, RO_GS>(ctx, r0, r1, A.rowptr, A.cols, A.vals, S.X32[level].get(), S.X32[level].get(),
-                                      S.R32[level].get(), nullptr, k, "mrhs gauss-seidel class");
+                                      S.R32[level].get(), nullptr, k, len, "mrhs gauss-seidel class");
         }
       } else {
         CSRView<double> A = L.A<double>();
         if (L.overflow && q == K - 1) {
           rows_m<double, double, RO_JAC>(ctx, r0, r1, A.rowptr, A.cols, A.vals, S.X[level].get(), S.T[level].get(),
-                                         S.R[level].get(), L.l1d.get(), k, "mrhs l1-jacobi");
+                                         S.R[level].get(), L.l1d.get(), k, len, "mrhs l1-jacobi");
           k_copy<double><<<grid_for((r1 - r0) * k, BLK), BLK, 0, ctx->stream>>>((r1 - r0) * k, S.T[level].get(),
                                                                                 S.X[level].get() + r0 * k);
           check_launch(ctx, "mrhs copy");
         } else {
           rows_m<double, double, RO_GS>(ctx, r0, r1, A.rowptr, A.cols, A.vals, S.X[level].get(), S.X[level].get(),
-                                        S.R[level].get(), nullptr, k, "mrhs gauss-seidel class");
+                                        S.R[level].get(), nullptr, k, len, "mrhs gauss-seidel class");
         }
       }
     }

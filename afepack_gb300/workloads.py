@@ -81,18 +81,28 @@ def poisson3d_p1(n: int = 64, seed: int = 1) -> Workload:
     return Workload(f"poisson3d_p1_{n}", sp, None, f, *ACC[(3, 1)])
 
 
-def gaussian_sources(space: FESpace, count: int, seed: int = 5) -> np.ndarray:
-    """Nodal data of `count` requests on one 3D space, each drawn like the
-    64^3 Poisson workload's f: a sum of 8 Gaussians with centres U[0.2,0.8]^3
-    and widths U[0.05,0.2], request j from default_rng([seed, j])."""
-    x = space.dof_point
-    out = np.zeros((space.n_dof, count))
+def gaussian_sources(space: FESpace, count: int, seed: int = 5, device=None):
+    """Nodal data of `count` requests on one space, each drawn like the 64^3
+    Poisson workload's f: a sum of 8 Gaussians with centres U[0.2,0.8]^d and
+    widths U[0.05,0.2], request j from default_rng([seed, j]).  Returns an
+    n x count array, or a torch tensor on `device` (evaluated there)."""
+    if device is None:
+        x = space.dof_point
+        out = np.zeros((space.n_dof, count))
+    else:
+        import torch
+        x = torch.from_numpy(np.ascontiguousarray(space.dof_point)).to(device)
+        out = torch.zeros((space.n_dof, count), dtype=torch.float64, device=device)
     for j in range(count):
         rng = np.random.default_rng([seed, j])
-        centres = rng.uniform(0.2, 0.8, size=(8, x.shape[1]))
+        centres = rng.uniform(0.2, 0.8, size=(8, space.dof_point.shape[1]))
         widths = rng.uniform(0.05, 0.2, size=8)
         for c, s in zip(centres, widths):
-            out[:, j] += np.exp(-np.sum((x - c) ** 2, axis=1) / (2.0 * s * s))
+            if device is None:
+                out[:, j] += np.exp(-np.sum((x - c) ** 2, axis=1) / (2.0 * s * s))
+            else:
+                ct = torch.as_tensor(c, dtype=torch.float64, device=device)
+                out[:, j] += torch.exp(-((x - ct) ** 2).sum(dim=1) / (2.0 * s * s))
     return out
 
 

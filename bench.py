@@ -294,11 +294,11 @@ def run_ours(args):
     from afepack_gb300.serve import BatchServer
     Wd = args.width
     nreq_dev = Wd * (max(args.warmup, 3) + args.steps)
-    F = W.gaussian_sources(wl.space, nreq_dev + args.served, seed=5)
+    F = W.gaussian_sources(wl.space, nreq_dev + args.served, seed=5, device=dev)
     dmask = torch.from_numpy((wl.space.dof_bmark != 0)).to(dev)
     Bcols = []
     for j in range(F.shape[1]):
-        bj = M.vmult(torch.from_numpy(np.ascontiguousarray(F[:, j])).to(dev))
+        bj = M.vmult(F[:, j].contiguous())
         bj[dmask] = 0.0
         Bcols.append(bj)
     blocks = [torch.stack(Bcols[i * Wd:(i + 1) * Wd], dim=1).contiguous() for i in range(nreq_dev // Wd)]
