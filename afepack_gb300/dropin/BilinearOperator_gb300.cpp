@@ -7,23 +7,29 @@
 // BilinearOperator<D, double, double, D, D, D>::build() (include/AFEPack/
 // BilinearOperator.templates.h:56-60) is specialised for D = 2, 3.  When the
 // object's exact dynamic type is StiffMatrix<D, double> or MassMatrix<D,
-// double> -- not a user subclass that overrides getElementMatrix -- and its
-// space uses the Lagrange P1/P2 triangle or tetrahedron templates, the mesh
-// and DOF map go to afp_space_create, afp_assemble builds the matrix on the
-// GPU (pattern and values bitwise the reference's), and the result is copied
-// into the object's own SparsityPattern and SparseMatrix storage, which then
-// hold exactly what the reference's build() would have produced.  GPU
-// failures abort with a message (the reference's own failures assert or
-// abort); there is no CPU path for these operators.  Every other operator
-// (user getElementMatrix, other templates or value types) keeps the
-// reference's build(): those are outside the GPU path.
+// double> -- not a user subclass that overrides getElementMatrix -- and every
+// element's template takes its basis functions from AFEPack's Lagrange P1/P2
+// triangle or tetrahedron plugin (libtriangle.{1,2}.bas_fun.so,
+// libtetrahedron.{1,2}.bas_fun.so, read from the template's own basis
+// function records), the mesh and DOF map go to afp_space_create,
+// afp_assemble builds the matrix on the GPU (pattern and values bitwise the
+// reference's), and the result is copied into the object's own
+// SparsityPattern and SparseMatrix storage, which then hold exactly what the
+// reference's build() would have produced.  Any other scalar operator of
+// these two instantiations (a user getElementMatrix, another template such as
+// the discontinuous P1 triangle, which also has 3 DOFs) is refused with a
+// message and abort(): there is no CPU path for them in this build.  GPU
+// failures abort too (the reference's own failures assert or abort).
 //
 // The file also provides the explicit instantiations that the replaced file
-// provides, so the library links unchanged.  AFP_DEVICE selects the GPU.
+// provides, so the library links unchanged (the vector-valued operators keep
+// the header's generic build()).  AFP_DEVICE selects the GPU.
 #include <AFEPack/BilinearOperator.templates.h>
 
 #include <cstdlib>
 #include <iostream>
+#include <sstream>
+#include <string>
 #include <typeinfo>
 #include <vector>
 
@@ -50,11 +56,47 @@ afp_context* context() {
   return g_ctx;
 }
 
-// Polynomial degree of a Lagrange template with nd DOFs on the D-simplex (0 if
-// the GPU path does not cover it).
-int lagrange_degree(int D, int nd) {
-  if (D == 2) return nd == 3 ? 1 : nd == 6 ? 2 : 0;
-  return nd == 4 ? 1 : nd == 10 ? 2 : 0;
+// Polynomial degree of the Lagrange template whose basis functions come from
+// the plugin library `lib` on the D-simplex (0 if it is not one the GPU path
+// covers).  The library name is the first field of a basis function record
+// as BasisFunction's stream output writes it (TemplateElement.h:181-191).
+int lagrange_degree(int D, const std::string& lib) {
+  const std::string base = lib.substr(lib.find_last_of('/') == std::string::npos ? 0 : lib.find_last_of('/') + 1);
+  if (D == 2) return base == "libtriangle.1.bas_fun.so" ? 1 : base == "libtriangle.2.bas_fun.so" ? 2 : 0;
+  return base == "libtetrahedron.1.bas_fun.so" ? 1 : base == "libtetrahedron.2.bas_fun.so" ? 2 : 0;
+}
+
+template <class BF>
+std::string plugin_library(const BF& bf) {
+  std::ostringstream os;
+  os << bf;  // interpolation point, then "library\tvalue\tgradient"
+  std::istringstream is(os.str());
+  std::string tok, lib;
+  while (is >> tok)
+    if (tok.size() > 3 && tok.compare(tok.size() - 3, 3, ".so") == 0) lib = tok;
+  return lib;
+}
+
+// Degree of the template every element uses when it is one P1 or P2 plugin
+// throughout, else 0.
+template <int D, class Space>
+int space_degree(const Space& sp) {
+  const int ne = sp.n_element();
+  int degree = -1;
+  for (int e = 0; e < ne; ++e) {
+    const auto& tmpl = sp.element(e).templateElement();
+    const int nd = (int)tmpl.n_dof();
+    int deg = -1;
+    for (int i = 0; i < nd; ++i) {
+      const int d = lagrange_degree(D, plugin_library(tmpl.basisFunction(i)));
+      if (d == 0 || (deg >= 0 && d != deg)) return 0;
+      deg = d;
+    }
+    const int expect = D == 2 ? (deg == 1 ? 3 : 6) : (deg == 1 ? 4 : 10);
+    if (nd != expect || (degree >= 0 && deg != degree)) return 0;
+    degree = deg;
+  }
+  return degree < 0 ? 0 : degree;
 }
 
 // Assembles `op` on the GPU when it is a plain StiffMatrix / MassMatrix on a
@@ -68,9 +110,9 @@ bool gpu_build(BilinearOperator<D, double, double, D, D, D>& op) {
   if (sp == nullptr || sp != op.FEMSpace1()) return false;
   const int ne = sp->n_element();
   if (ne == 0) return false;
-  const int nd = (int)sp->element(0).n_dof();
-  const int degree = lagrange_degree(D, nd);
+  const int degree = space_degree<D>(*sp);
   if (degree == 0) return false;
+  const int nd = (int)sp->element(0).n_dof();
   Mesh<D, D>& mesh = sp->mesh();
   std::vector<int32_t> cells((size_t)ne * (D + 1)), elem_dof((size_t)ne * nd);
   for (int e = 0; e < ne; ++e) {
@@ -131,18 +173,23 @@ bool gpu_build(BilinearOperator<D, double, double, D, D, D>& op) {
 
 }  // namespace
 
+// An operator the GPU path does not cover: refused (no CPU path in this build).
+[[noreturn]] static void refuse(const char* type) {
+  std::cerr << "afepack_gb300: BilinearOperator::build() of " << type
+            << " is not on the GPU path (StiffMatrix / MassMatrix on AFEPack's Lagrange P1/P2 triangle or "
+               "tetrahedron templates); link the reference's src/BilinearOperator.cpp for other operators"
+            << std::endl;
+  abort();
+}
+
 template <>
 void BilinearOperator<2, double, double, 2, 2, 2>::build() {
-  if (gpu_build<2>(*this)) return;
-  buildSparsityPattern();
-  buildSparseMatrix();
+  if (!gpu_build<2>(*this)) refuse(typeid(*this).name());
 }
 
 template <>
 void BilinearOperator<3, double, double, 3, 3, 3>::build() {
-  if (gpu_build<3>(*this)) return;
-  buildSparsityPattern();
-  buildSparseMatrix();
+  if (!gpu_build<3>(*this)) refuse(typeid(*this).name());
 }
 
 // The instantiations of the replaced src/BilinearOperator.cpp: scalar

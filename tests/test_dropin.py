@@ -51,7 +51,7 @@ def test_dropin_links_into_afepack(native, tmp_path):
     flags = ["-std=c++20", "-O1", "-w", "-I" + os.path.join(ROOT, "oracle", "shim"), "-I" + os.path.join(REF, "include"),
              "-I" + os.path.join(ROOT, "include")]
     drops = []
-    for src in ("AMGSolver_gb300.cpp", "BilinearOperator_gb300.cpp"):
+    for src in ("AMGSolver_gb300.cpp", "BilinearOperator_gb300.cpp", "dropin_core.cpp"):
         obj = tmp_path / src.replace(".cpp", ".o")
         subprocess.check_call(["g++", *flags, "-c", os.path.join(ROOT, "afepack_gb300", "dropin", src), "-o", str(obj)])
         drops.append(str(obj))
