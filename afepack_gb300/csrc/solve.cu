@@ -494,6 +494,67 @@ __global__ void k_gj_eliminate(int64_t n, int64_t c, double* __restrict__ M, dou
   A[r * n + k] -= f * A[c * n + k];
 }
 
+// C = alpha A B + beta C in FP64 (row-major, leading dimensions lda, ldb,
+// ldc): 64 x 64 output tiles, 16-deep steps of k staged in shared memory,
+// 4 x 4 outputs per thread (rows ty + 16a, columns tx + 16b).
+__global__ void __launch_bounds__(256) k_dgemm(int64_t m, int64_t n, int64_t k, double alpha,
+                                               const double* __restrict__ A, int64_t lda,
+                                               const double* __restrict__ B, int64_t ldb, double beta,
+                                               double* __restrict__ C, int64_t ldc) {
+  __shared__ double As[16][65];
+  __shared__ double Bs[16][64];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int64_t row0 = (int64_t)blockIdx.y * 64, col0 = (int64_t)blockIdx.x * 64;
+  double acc[4][4] = {};
+  for (int64_t k0 = 0; k0 < k; k0 += 16) {
+    for (int q = threadIdx.x; q < 64 * 16; q += 256) {
+      const int r = q / 16, c = q % 16;
+      As[c][r] = (row0 + r < m && k0 + c < k) ? A[(row0 + r) * lda + k0 + c] : 0.0;
+      const int br = q / 64, bc = q % 64;
+      Bs[br][bc] = (k0 + br < k && col0 + bc < n) ? B[(k0 + br) * ldb + col0 + bc] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t r = row0 + ty + 16 * i, c = col0 + tx + 16 * j;
+      if (r < m && c < n) C[r * ldc + c] = alpha * acc[i][j] + (beta == 0.0 ? 0.0 : beta * C[r * ldc + c]);
+    }
+}
+
+// dst[i][j] = src[i][j] for i < rows, j < cols (row-major, leading dims);
+// rows [z0, z1) of dst get zeros instead (z1 <= z0: none).
+__global__ void k_copy2d(int64_t rows, int64_t cols, const double* __restrict__ src, int64_t lds,
+                         double* __restrict__ dst, int64_t ldd, int64_t z0, int64_t z1) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= rows * cols) return;
+  const int64_t i = t / cols, j = t % cols;
+  dst[i * ldd + j] = (i >= z0 && i < z1) ? 0.0 : src[i * lds + j];
+}
+
+// columns [c0, c1) of a rows x cols row-major block set to zero
+__global__ void k_zero_cols(int64_t rows, int64_t cols, double* __restrict__ M, int64_t c0, int64_t c1) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t w = c1 - c0;
+  if (t >= rows * w) return;
+  M[(t / w) * cols + c0 + t % w] = 0.0;
+}
+
 template <class F>
 void launch_vec(int vec, F&& f) {
   switch (vec) {
@@ -663,26 +724,88 @@ void l1_diag(const afp_context* ctx, const CSRView<double>& A, int64_t r0, int64
   check_launch(ctx, "l1 diagonal");
 }
 
-bool dense_inverse(const afp_context* ctx, const CSRView<double>& A, double* inv) {
-  const int64_t n = A.m;
-  DevBuf<double> M(ctx, n * n), colc(ctx, n);
+namespace {
+
+// inv = M^-1 for a dense n x n row-major M (overwritten) by Gauss-Jordan
+// elimination with partial pivoting, two launches per column; false when a
+// pivot is zero.
+bool gj_inverse(const afp_context* ctx, int64_t n, double* M, double* inv) {
+  DevBuf<double> colc(ctx, n);
   DevBuf<int> singular(ctx, 1);
   singular.zero();
-  M.zero();
-  k_csr_to_dense<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, A.rowptr, A.cols, A.vals, M.get());
-  check_launch(ctx, "dense copy");
   k_identity<<<grid_for(n * n, BLK), BLK, 0, ctx->stream>>>(n, inv);
   check_launch(ctx, "identity");
   for (int64_t c = 0; c < n; ++c) {
-    k_gj_pivot<<<1, 1024, 0, ctx->stream>>>(n, c, M.get(), inv, colc.get(), singular.get());
+    k_gj_pivot<<<1, 1024, 0, ctx->stream>>>(n, c, M, inv, colc.get(), singular.get());
     check_launch(ctx, "gauss-jordan pivot");
-    k_gj_eliminate<<<grid_for(2 * n * n, BLK), BLK, 0, ctx->stream>>>(n, c, M.get(), inv, colc.get(), singular.get());
+    k_gj_eliminate<<<grid_for(2 * n * n, BLK), BLK, 0, ctx->stream>>>(n, c, M, inv, colc.get(), singular.get());
     check_launch(ctx, "gauss-jordan eliminate");
   }
   int hs = 0;
   singular.download(&hs, 1);
   sync(ctx);
   return hs == 0;
+}
+
+void dgemm(const afp_context* ctx, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+           const double* B, int64_t ldb, double beta, double* C, int64_t ldc) {
+  if (m == 0 || n == 0) return;
+  dim3 grid((unsigned)((n + 63) / 64), (unsigned)((m + 63) / 64));
+  k_dgemm<<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  check_launch(ctx, "dgemm");
+}
+
+void copy2d(const afp_context* ctx, int64_t rows, int64_t cols, const double* src, int64_t lds, double* dst,
+            int64_t ldd, int64_t z0 = 0, int64_t z1 = 0) {
+  if (rows * cols == 0) return;
+  k_copy2d<<<grid_for(rows * cols, BLK), BLK, 0, ctx->stream>>>(rows, cols, src, lds, dst, ldd, z0, z1);
+  check_launch(ctx, "copy block");
+}
+
+}  // namespace
+
+// Dense inverse of an SPD matrix (the coarsest level of the hierarchy).  Up
+// to kPanel rows: Gauss-Jordan with partial pivoting.  Larger: the blocked
+// sweep in place on the output, kPanel pivots at a time -- with the block
+// pivot P, the panel rows R, the panel columns C and the rest S,
+//   P <- P^-1,  R <- P^-1 R,  S <- S - C P^-1 R,  C <- -C P^-1,
+// which after every panel leaves the inverse; the updates are FP64 GEMMs
+// (2 n^3 flops in all).  A symmetric positive definite matrix needs no
+// pivoting across panels (every block pivot is a Schur complement of it,
+// itself SPD); within a pivot block the Gauss-Jordan pivots rows.
+bool dense_inverse(const afp_context* ctx, const CSRView<double>& A, double* inv) {
+  constexpr int64_t kPanel = 512;
+  const int64_t n = A.m;
+  if (n <= kPanel) {
+    DevBuf<double> M(ctx, n * n);
+    M.zero();
+    k_csr_to_dense<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, A.rowptr, A.cols, A.vals, M.get());
+    check_launch(ctx, "dense copy");
+    return gj_inverse(ctx, n, M.get(), inv);
+  }
+  AFP_CUDA(cudaMemsetAsync(inv, 0, sizeof(double) * n * n, ctx->stream));
+  k_csr_to_dense<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, A.rowptr, A.cols, A.vals, inv);
+  check_launch(ctx, "dense copy");
+  const int64_t b = kPanel;
+  DevBuf<double> Pm(ctx, b * b), Pi(ctx, b * b), Rnew(ctx, b * n), Ccol(ctx, n * b), Crow(ctx, b * n);
+  for (int64_t k0 = 0; k0 < n; k0 += b) {
+    const int64_t k1 = std::min(n, k0 + b), pb = k1 - k0;
+    copy2d(ctx, pb, pb, inv + k0 * n + k0, n, Pm.get(), pb);                   // P
+    if (!gj_inverse(ctx, pb, Pm.get(), Pi.get())) return false;                 // P^-1
+    copy2d(ctx, pb, n, inv + k0 * n, n, Crow.get(), n);                         // R (whole panel rows)
+    copy2d(ctx, n, pb, inv + k0, n, Ccol.get(), pb, k0, k1);                    // C (panel rows zeroed)
+    dgemm(ctx, pb, n, pb, 1.0, Pi.get(), pb, Crow.get(), n, 0.0, Rnew.get(), n);  // P^-1 R
+    k_zero_cols<<<grid_for(pb * pb, BLK), BLK, 0, ctx->stream>>>(pb, n, Rnew.get(), k0, k1);
+    check_launch(ctx, "zero panel columns");
+    dgemm(ctx, n, n, pb, -1.0, Ccol.get(), pb, Rnew.get(), n, 1.0, inv, n);    // S - C P^-1 R
+    copy2d(ctx, pb, n, Rnew.get(), n, inv + k0 * n, n);                         // panel rows
+    copy2d(ctx, pb, pb, Pi.get(), pb, inv + k0 * n + k0, n);                    // pivot block
+    dgemm(ctx, n, pb, pb, -1.0, Ccol.get(), pb, Pi.get(), pb, 0.0, Crow.get(), pb);  // -C P^-1 (into Crow)
+    copy2d(ctx, n, pb, Crow.get(), pb, inv + k0, n, k0, k1);                    // panel columns...
+    copy2d(ctx, pb, pb, Pi.get(), pb, inv + k0 * n + k0, n);                    // ...except the pivot block
+  }
+  sync(ctx);
+  return true;
 }
 
 void csr_spmv(const afp_context* ctx, int64_t m, const int* rowptr, const int* cols, const double* vals,
