@@ -491,8 +491,22 @@ void setup(afp_amg* h, afp_matrix* A, bool lazy) {
     const double* ava = l == 0 ? A->vals.get() : refDev[l].va.get();
     Pattern cpat;
     DevBuf<double> cvals;
-    galerkin_product(ctx, P.m, P.n, dP.rp.get(), dP.ci.get(), dP.va.get(), arp, aci, ava, dT.rp.get(), dT.ci.get(),
-                     dT.va.get(), cpat, cvals);
+    // A coarse level small enough to become the dense tail (by rows, or by
+    // density up to kDenseTailMax rows) is formed through the dense product;
+    // if it then turns out not to be the tail, the reference-order product
+    // is formed after all (the next splitting needs getPMPt's values).
+    bool dense_done = false;
+    if (o.dense_tail > 0 && P.m <= kDenseTailMax) {
+      galerkin_product_dense(ctx, P.m, P.n, dP.rp.get(), dP.ci.get(), dP.va.get(), arp, aci, ava, dT.rp.get(),
+                             dT.ci.get(), dT.va.get(), cpat, cvals);
+      const double density = (double)cpat.nnz / ((double)P.m * (double)P.m);
+      dense_done = P.m <= o.dense_tail || density >= kDenseTailDensity;
+      tr.mark(ctx, dense_done ? "GPU Galerkin product (dense, tail)" : "GPU Galerkin product (dense, discarded)",
+              l + 1, cpat.m, cpat.nnz);
+    }
+    if (!dense_done)
+      galerkin_product(ctx, P.m, P.n, dP.rp.get(), dP.ci.get(), dP.va.get(), arp, aci, ava, dT.rp.get(), dT.ci.get(),
+                       dT.va.get(), cpat, cvals);
     tr.mark(ctx, "GPU Galerkin product", l + 1, cpat.m, cpat.nnz);
     HostCSR C;
     download_host_csr(ctx, cpat.m, cpat.n, cpat.nnz, cpat.rowptr.get(), cpat.cols.get(), cvals.get(), C);

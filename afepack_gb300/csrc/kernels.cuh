@@ -21,6 +21,14 @@ void galerkin_product(const afp_context* ctx, int64_t n_c, int64_t n_f, const in
 // current device); called once per context creation (noalloc.cu).
 void noalloc_reserve(int device);
 
+// The same product through a dense intermediate (n_f x n_c and n_c x n_c
+// FP64 arrays), for the dense-tail level only: deterministic, but not
+// getPMPt's accumulation order; exact zeros other than the diagonal dropped.
+void galerkin_product_dense(const afp_context* ctx, int64_t n_c, int64_t n_f, const int* p_rowptr,
+                            const int* p_cols, const double* p_vals, const int* a_rowptr, const int* a_cols,
+                            const double* a_vals, const int* pt_rowptr, const int* pt_cols, const double* pt_vals,
+                            Pattern& out_pat, DevBuf<double>& out_vals);
+
 // Host CSR (AFEPack layout) used by the coarsening.
 struct HostCSR {
   int64_t m = 0, n = 0;

@@ -314,3 +314,99 @@ void galerkin_product(const afp_context* ctx, int64_t n_c, int64_t n_f, const in
 }
 
 }  // namespace afp
+
+// ------------------------------------------------------------------------
+// Galerkin product of the dense tail.  The coarsest level is only inverted,
+// never split again, so it does not need getPMPt's accumulation order; with
+// at most a few thousand coarse rows it is formed through a dense
+// intermediate instead: T = A P^T (n_f x n_c, one thread per row of A,
+// accumulating in A's and then P^T's entry order), then A_c = P T (one block
+// per coarse row, P's entry order), both FP64 and deterministic.  The result
+// is returned in AFEPack's CSR layout (diagonal first, then ascending),
+// keeping the entries that are not exactly zero.
+namespace afp {
+namespace {
+
+__global__ void k_rap_dense_t(int64_t nf, int64_t nc, const int* __restrict__ arp, const int* __restrict__ ac,
+                              const double* __restrict__ av, const int* __restrict__ trp,
+                              const int* __restrict__ tc, const double* __restrict__ tv, double* __restrict__ T) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nf) return;
+  double* Ti = T + i * nc;
+  for (int q = arp[i]; q < arp[i + 1]; ++q) {
+    const double a = av[q];
+    const int k = ac[q];
+    for (int s = trp[k]; s < trp[k + 1]; ++s) Ti[tc[s]] += a * tv[s];
+  }
+}
+
+__global__ void k_rap_dense_pt(int64_t nc, const int* __restrict__ prp, const int* __restrict__ pc,
+                               const double* __restrict__ pv, const double* __restrict__ T, double* __restrict__ Ac) {
+  const int64_t c = blockIdx.x;
+  const int b = prp[c], e = prp[c + 1];
+  for (int64_t j = threadIdx.x; j < nc; j += blockDim.x) {
+    double s = 0.0;
+    for (int q = b; q < e; ++q) s += pv[q] * T[(int64_t)pc[q] * nc + j];
+    Ac[c * nc + j] = s;
+  }
+}
+
+// entries of dense row c that are kept: the diagonal always, others if != 0
+__global__ void k_dense_row_count(int64_t n, const double* __restrict__ D, int* __restrict__ cnt) {
+  const int64_t c = blockIdx.x;
+  int local = 0;
+  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) local += (j == c || D[c * n + j] != 0.0) ? 1 : 0;
+  __shared__ int red[256];
+  red[threadIdx.x] = local;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) cnt[c] = red[0];
+}
+
+// one thread per row: the diagonal first, then the others in ascending order
+__global__ void k_dense_row_fill(int64_t n, const double* __restrict__ D, const int* __restrict__ rp,
+                                 int* __restrict__ ci, double* __restrict__ va) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  int o = rp[c];
+  ci[o] = (int)c;
+  va[o] = D[c * n + c];
+  ++o;
+  for (int64_t j = 0; j < n; ++j)
+    if (j != c && D[c * n + j] != 0.0) {
+      ci[o] = (int)j;
+      va[o] = D[c * n + j];
+      ++o;
+    }
+}
+
+}  // namespace
+
+void galerkin_product_dense(const afp_context* ctx, int64_t n_c, int64_t n_f, const int* prp, const int* pc,
+                            const double* pv, const int* arp, const int* ac, const double* av, const int* trp,
+                            const int* tc, const double* tv, Pattern& out, DevBuf<double>& vals) {
+  DevBuf<double> T(ctx, n_f * n_c), D(ctx, n_c * n_c);
+  T.zero();
+  k_rap_dense_t<<<grid_for(n_f, 128), 128, 0, ctx->stream>>>(n_f, n_c, arp, ac, av, trp, tc, tv, T.get());
+  check_launch(ctx, "dense Galerkin A P^T");
+  k_rap_dense_pt<<<(unsigned)n_c, 256, 0, ctx->stream>>>(n_c, prp, pc, pv, T.get(), D.get());
+  check_launch(ctx, "dense Galerkin P (A P^T)");
+  T = DevBuf<double>();
+  DevBuf<int> cnt(ctx, n_c);
+  k_dense_row_count<<<(unsigned)n_c, 256, 0, ctx->stream>>>(n_c, D.get(), cnt.get());
+  check_launch(ctx, "dense row count");
+  out.m = out.n = n_c;
+  out.rowptr.alloc(ctx, n_c + 1);
+  out.nnz = exclusive_scan(ctx, cnt.get(), out.rowptr.get(), n_c);
+  out.cols.alloc(ctx, out.nnz);
+  vals.alloc(ctx, out.nnz);
+  k_dense_row_fill<<<grid_for(n_c, 128), 128, 0, ctx->stream>>>(n_c, D.get(), out.rowptr.get(), out.cols.get(),
+                                                                 vals.get());
+  check_launch(ctx, "dense row fill");
+  sync(ctx);
+}
+
+}  // namespace afp
