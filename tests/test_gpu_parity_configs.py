@@ -65,3 +65,48 @@ def test_bf16_interpolation_reaches_the_direct_solution(ctx):
         it[name] = info["iterations"]
     # BF16 interpolation weights cost iterations, within a bound
     assert it["bf16"] <= 2 * it["fp64"] + 5, it
+
+
+def test_elliptic2d_p2_512_mixed_against_direct(ctx):
+    """2D P2 on the 512^2 split grid (1,050,625 DOFs), coefficient contrast
+    1e4: the mixed-precision solve against SuperLU."""
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import MIXED, AMGSolver
+    wl = W.elliptic2d_p2(512)
+    K, b = system(ctx, wl)
+    amg = AMGSolver(K, precision=MIXED)
+    x, info = amg.pcg(b, 1e-10, 2000)
+    assert info["converged"], info
+    xd = spla.splu(scipy_matrix(K).tocsc()).solve(b)
+    assert np.linalg.norm(x - xd) <= 1e-8 * np.linalg.norm(xd)
+
+
+def test_poisson3d_p2_48_batched_against_oracle(ctx):
+    """3D P2 on the 48^3 Kuhn cube (912,673 DOFs), 64 right-hand sides, the
+    reference's lazyProject hierarchy: batched mixed-precision CG against the
+    oracle's FP64 CG (the reference algorithm in C, on its own lazy
+    hierarchy) for two of the columns."""
+    import oracle as O
+    import torch
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import MIXED, AMGSolver
+    from afepack_gb300.fem import BoundaryConditionAdmin, Space, assemble
+    wl = W.poisson3d_p2_multi(48, 64)
+    K, M = assemble(Space(ctx, wl.space), wl.acc_stiff, wl.acc_mass)
+    d = wl.space.dof_bmark != 0
+    Bm = np.stack([M.vmult(np.ascontiguousarray(wl.f[:, c])) for c in range(64)], axis=1)
+    bca = BoundaryConditionAdmin(wl.space)
+    bca.add(1, 0.0)
+    bca.apply(K, np.ascontiguousarray(Bm[:, 0]).copy())
+    Bm[d] = 0.0
+    amg = AMGSolver(precision=MIXED)
+    amg.lazyReinit(K)
+    X, infos = amg.pcg_multi(torch.from_numpy(np.ascontiguousarray(Bm)).to("cuda:0"), 1e-10, 500)
+    assert all(i["converged"] for i in infos)
+    X = X.cpu().numpy()
+    rp, ci, va = K.download()
+    ref = O.AMG.lazy(O.CSR(rp, ci, va, (rp.shape[0] - 1,) * 2))
+    for c in (0, 63):
+        xo, it, rel = ref.pcg(np.ascontiguousarray(Bm[:, c]), 1e-12, 500)
+        assert rel <= 1e-12
+        assert np.linalg.norm(X[:, c] - xo) <= 1e-8 * np.linalg.norm(xo), c
