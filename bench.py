@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--width", type=int, default=64, help="requests per batched step / batch-server columns")
     ap.add_argument("--served", type=int, default=256, help="requests sent through the batch server")
     ap.add_argument("--stream", action="store_true", help="served request stream instead of one workload")
-    ap.add_argument("--stream-sample", type=int, default=48)
+    ap.add_argument("--stream-sample", type=int, default=200)
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--multi", action="store_true", help="batched multi-RHS workload (3D P2, 64 RHS)")
     ap.add_argument("--multi-n", type=int, default=48)
@@ -527,50 +527,65 @@ def run_multi(args):
 
 
 def run_stream(args):
-    """Served stream (independent 2D P1 requests, n log-uniform in [32,1024],
-    half variable-coefficient): a bounded sample of the stream is submitted at
-    once (saturation) to the solve server, mixed precision and FP64."""
+    """Served stream of independent meshes (2D P1, n log-uniform in
+    [32, 1024], half variable-coefficient, seed 4): every 10th of the 2000
+    requests (200, a stratified sample of the stream) through the solve
+    server (afp_server_*: 8 execution slots, HBM admission, each request's
+    whole path -- assembly, AMG setup, CG -- on the GPU), first all at once
+    (saturation), then with Poisson arrivals at 50% of that rate; mixed
+    precision and FP64."""
     from afepack_gb300 import workloads as W
     from afepack_gb300 import build as B
     from afepack_gb300.serve import Server
     B.build()
-    reqs = W.request_stream(2000, seed=4)[: args.stream_sample]
+    reqs = W.request_stream(2000, seed=4)[:: max(1, 2000 // args.stream_sample)]
     t0 = time.perf_counter()
     wls = [W.request_workload(r) for r in reqs]
     gen_s = time.perf_counter() - t0
     phase("stream: request generation")
+
+    def run(srv, arrivals):
+        srv.reset_stats()
+        t0 = time.perf_counter()
+        due, tickets = t0, []
+        for wl, g in zip(wls, arrivals):
+            due += g
+            while time.perf_counter() < due:
+                time.sleep(0.0005)
+            tickets.append(srv.submit(wl))
+        res = [srv.wait(t)[1] for t in tickets]
+        wall = time.perf_counter() - t0
+        lat = np.array([r["latency_seconds"] for r in res])
+        return {"requests": len(res), "solves_per_s": round(len(res) / wall, 3),
+                "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 1),
+                "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 1),
+                "failed": int(sum(r["status"] != 0 for r in res)),
+                "iterations_median": int(np.median([r["iterations"] for r in res]))}
+
     out = {}
     for name, prec in (("mixed", 1), ("fp64", 0)):
         with Server(workers=args.workers, precision=prec, tol=args.tol) as srv:
-            warm = [srv.submit(wl) for wl in wls[: min(4, len(wls))]]
-            for t in warm:
+            for t in [srv.submit(wl) for wl in wls[: min(4, len(wls))]]:
                 srv.wait(t)
-            srv.reset_stats()
-            s0 = time.perf_counter()
-            tickets = [srv.submit(wl) for wl in wls]
-            res = []
-            for i, t in enumerate(tickets):
-                res.append(srv.wait(t)[1])
-                print(f"[bench] stream {name}: request {i + 1}/{len(tickets)} done "
-                      f"({res[-1]['latency_seconds']:.2f} s, n_dof {int(wls[i].space.n_dof)})", file=sys.stderr, flush=True)
-            wall = time.perf_counter() - s0
-            st = srv.stats()
-            phase(f"stream: {name} server run")
-        lat = np.array([r["latency_seconds"] for r in res])
-        out[name] = {"solves_per_s": len(res) / wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
-                     "p99_ms": 1e3 * float(np.percentile(lat, 99)), "failed": int(st["failed"]),
-                     "iterations_median": int(np.median([r["iterations"] for r in res]))}
+            sat = run(srv, np.zeros(len(wls)))
+            rate = 0.5 * sat["solves_per_s"]
+            paced = run(srv, np.random.default_rng(11).exponential(1.0 / rate, len(wls)))
+            paced["arrival_rate_per_s"] = round(rate, 3)
+        out[name] = {"saturation": sat, "poisson_50pct": paced}
+        phase(f"stream: {name} server runs")
     ndofs = [int(w.space.n_dof) for w in wls]
+    m = out["mixed"]
     return {
-        "metric": METRIC, "value": round(out["mixed"]["solves_per_s"], 3), "unit": "solves/s", "n_gpus": 1,
+        "metric": METRIC, "value": m["saturation"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
         "steps": 1, "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 V-cycle + fp64 CG", "data": "synthetic (seeded)",
-        "config": {"workload": "request_stream", "requests": len(wls), "workers": args.workers,
-                   "n_dof_min": min(ndofs), "n_dof_max": max(ndofs), "n_dof_total": sum(ndofs), "tol": args.tol,
-                   "arrival": "all at once (saturation)", "generation_s": round(gen_s, 2)},
-        "p50_ms": round(out["mixed"]["p50_ms"], 2), "p99_ms": round(out["mixed"]["p99_ms"], 2),
-        "fp64": out["fp64"], "mixed": out["mixed"],
-        "mixed_over_fp64": round(out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"], 3),
+        "config": {"workload": "request_stream", "requests": len(wls), "sample": "every 10th of the 2000-request stream",
+                   "workers": args.workers, "n_dof_min": min(ndofs), "n_dof_max": max(ndofs),
+                   "n_dof_total": sum(ndofs), "tol": args.tol, "generation_s": round(gen_s, 2),
+                   "arrival": "saturation (all at once), then Poisson at 50% of the saturated rate"},
+        "p50_ms": m["poisson_50pct"]["p50_ms"], "p99_ms": m["poisson_50pct"]["p99_ms"],
+        "mixed": m, "fp64": out["fp64"],
+        "mixed_over_fp64": round(m["saturation"]["solves_per_s"] / out["fp64"]["saturation"]["solves_per_s"], 3),
     }
 
 
