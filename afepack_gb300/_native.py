@@ -41,7 +41,7 @@ class AMGOpts(C.Structure):
                 ("min_density", C.c_double), ("alpha", C.c_double), ("precision", C.c_int),
                 ("dense_tail", C.c_int), ("max_colors", C.c_int), ("symmetric", C.c_int),
                 ("coarse_colors", C.c_int), ("interp_bf16", C.c_int),
-                ("fused_vcycle", C.c_int), ("wait_limit_s", C.c_double), ("inject_barrier_stall", C.c_int)]
+                ("fused_vcycle", C.c_int), ("wait_limit_s", C.c_double), ("inject_barrier_stall", C.c_int), ("gpu_coarsen", C.c_int)]
 
 
 class SolveInfo(C.Structure):

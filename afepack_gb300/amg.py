@@ -31,7 +31,7 @@ class AMGSolver:
     def __init__(self, M: SparseMatrix | None = None, tol: float = 1.0e-12, s: int = 3, nmpo: int = 50,
                  nmpsd: float = 0.382, alp: float = 0.25, *, precision: int = FP64, dense_tail: int | None = None,
                  max_colors: int | None = None, symmetric: bool = True, coarse_colors: int | None = None,
-                 interp_bf16: bool | None = None, fused_vcycle: bool | None = None):
+                 interp_bf16: bool | None = None, fused_vcycle: bool | None = None, gpu_coarsen: bool | None = None):
         self.opts = default_opts()
         self.opts.tolerance = tol
         self.opts.smooth_step = s
@@ -50,6 +50,8 @@ class AMGSolver:
             self.opts.interp_bf16 = int(interp_bf16)
         if fused_vcycle is not None:
             self.opts.fused_vcycle = int(fused_vcycle)
+        if gpu_coarsen is not None:
+            self.opts.gpu_coarsen = int(gpu_coarsen)
         self.handle = None
         self.matrix = None
         if M is not None:

@@ -25,6 +25,7 @@ SOURCES = [
     ("context.cu", []),
     ("assemble.cu", ["-fmad=false"]),
     ("rap.cu", ["-fmad=false"]),
+    ("coarsen.cu", ["-fmad=false"]),
     ("solve.cu", []),
     ("amg.cu", []),
     ("mrhs.cu", []),

@@ -38,11 +38,6 @@ namespace {
 constexpr int64_t kDenseTailMax = 16384;
 constexpr double kDenseTailDensity = 0.05;
 
-struct DevCSR {
-  int64_t m = 0, n = 0, nnz = 0;
-  DevBuf<int> rp, ci;
-  DevBuf<double> va;
-};
 
 // Setup trace: with AFP_SETUP_TRACE set, each setup step prints its wall
 // time (after a stream sync) to stderr.
@@ -477,18 +472,29 @@ void setup(afp_amg* h, afp_matrix* A, bool lazy) {
       if (m <= (uint64_t)o.dense_tail || (m <= (uint64_t)kDenseTailMax && density >= kDenseTailDensity)) break;
     }
     const HostCSR& M = h->refA[l];
-    std::vector<int> cf;
-    HostCSR P, Pt;
-    tr.mark(ctx, "previous level done", l, M.m, M.nnz());
-    if (lazy) host_lazy_project(M, P, Pt);
-    else host_project(M, o.alpha, cf, P, Pt);
-    tr.mark(ctx, "host C/F + P", l, P.m, P.nnz());
-    DevCSR dP, dT;
-    upload_host_csr(ctx, P, dP);
-    upload_host_csr(ctx, Pt, dT);
     const int* arp = l == 0 ? A->pat->rowptr.get() : refDev[l].rp.get();
     const int* aci = l == 0 ? A->pat->cols.get() : refDev[l].ci.get();
     const double* ava = l == 0 ? A->vals.get() : refDev[l].va.get();
+    HostCSR P, Pt;
+    DevCSR dP, dT;
+    tr.mark(ctx, "previous level done", l, M.m, M.nnz());
+    if (!lazy && o.gpu_coarsen) {
+      GpuProjection g;
+      gpu_project(ctx, M.m, arp, aci, ava, o.alpha, g);
+      dP = std::move(g.P);
+      dT = std::move(g.Pt);
+      download_host_csr(ctx, dP.m, dP.n, dP.nnz, dP.rp.get(), dP.ci.get(), dP.va.get(), P);
+      if (tr.on)
+        std::fprintf(stderr, "[afp setup] level %d: C/F rounds %d + %d\n", l, g.rounds1, g.rounds2);
+      tr.mark(ctx, "GPU C/F + P", l, P.m, P.nnz());
+    } else {
+      std::vector<int> cf;
+      if (lazy) host_lazy_project(M, P, Pt);
+      else host_project(M, o.alpha, cf, P, Pt);
+      tr.mark(ctx, "host C/F + P", l, P.m, P.nnz());
+      upload_host_csr(ctx, P, dP);
+      upload_host_csr(ctx, Pt, dT);
+    }
     Pattern cpat;
     DevBuf<double> cvals;
     // A coarse level small enough to become the dense tail (by rows, or by
@@ -795,6 +801,7 @@ void afp_amg_default_opts(afp_amg_opts* o) {
   o->fused_vcycle = 0;
   o->wait_limit_s = 2.0;
   o->inject_barrier_stall = 0;
+  o->gpu_coarsen = 1;
 }
 
 afp_status afp_amg_setup(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out) {
@@ -808,7 +815,7 @@ afp_status afp_amg_setup(afp_matrix* a, const afp_amg_opts* opts, afp_amg** out)
     const afp_amg_opts& o = h->opts;
     AFP_REQUIRE(o.smooth_step >= 0 && o.max_coarse >= 1 && o.alpha >= 0 && o.max_colors >= 1 && o.dense_tail >= 0 &&
                     (o.precision == AFP_PRECISION_FP64 || o.precision == AFP_PRECISION_MIXED) &&
-                    o.wait_limit_s > 0 && o.wait_limit_s <= 60,
+                    o.wait_limit_s > 0 && o.wait_limit_s <= 60 && (o.gpu_coarsen == 0 || o.gpu_coarsen == 1),
                 AFP_ERR_INVALID, "invalid AMG options");
     AFP_REQUIRE(o.dense_tail <= 16384, AFP_ERR_UNSUPPORTED, "dense_tail above 16384 rows");
     setup(h.get(), a, false);

@@ -37,6 +37,24 @@ struct HostCSR {
   int64_t nnz() const { return rowptr.empty() ? 0 : rowptr[m]; }
 };
 
+// A device CSR (AFEPack layout for square levels, ascending rows for P, P^T).
+struct DevCSR {
+  int64_t m = 0, n = 0, nnz = 0;
+  DevBuf<int> rp, ci;
+  DevBuf<double> va;
+};
+
+// Project() on the GPU (coarsen.cu): flags and P, P^T bitwise the host
+// routine's; cf[i] = 1 for C points, 0 for F points; rounds of the two
+// passes for the trace.
+struct GpuProjection {
+  DevCSR P, Pt;
+  DevBuf<int> cf;
+  int rounds1 = 0, rounds2 = 0;
+};
+int gpu_project(const afp_context* ctx, int64_t m, const int* rowptr, const int* cols, const double* vals,
+                double alpha, GpuProjection& out);
+
 // Project(): C/F splitting and projection P (n_c x m) of one level, with
 // its transpose; cf[i] = -1 (C) or 1 (F).
 void host_project(const HostCSR& M, double alpha, std::vector<int>& cf, HostCSR& P, HostCSR& Pt);

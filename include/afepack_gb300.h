@@ -189,6 +189,9 @@ typedef struct afp_amg_opts {
                            barrier of each persistent V-cycle waits for one
                            arrival more than the grid has, so every wait runs
                            out after wait_limit_s (default 0) */
+  int gpu_coarsen;      /* classical hierarchy: C/F splitting and P on the GPU
+                           (1, default), with the host routine's flags and P
+                           bit for bit, or on the host (0) */
 } afp_amg_opts;
 
 typedef struct afp_solve_info {

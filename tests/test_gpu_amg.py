@@ -60,6 +60,34 @@ def test_hierarchy_matches_oracle_poisson2d(ctx):
         assert np.array_equal(arp, A.rowptr) and np.array_equal(aci, A.cols) and np.array_equal(ava, A.vals)
 
 
+@pytest.mark.parametrize("case", ["poisson2d_p1_256", "poisson3d_p1_24", "elliptic2d_p2_64", "poisson3d_p2_8"])
+def test_gpu_coarsening_matches_host(ctx, case):
+    """The GPU C/F splitting and P (gpu_coarsen=1) against the host routine
+    (gpu_coarsen=0) on every level of the full-depth hierarchy, bit for bit,
+    and level 0 against the oracle's Project."""
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import AMGSolver
+    wl = {"poisson2d_p1_256": lambda: W.poisson2d_p1(256),
+          "poisson3d_p1_24": lambda: W.poisson3d_p1(24),
+          "elliptic2d_p2_64": lambda: W.elliptic2d_p2(64),
+          "poisson3d_p2_8": lambda: W.poisson3d_p2_multi(8, 1)}[case]()
+    if wl.f.ndim == 2:
+        wl.f = wl.f[:, 0].copy()
+    _, K, _ = system(ctx, wl)
+    gpu = AMGSolver(K, dense_tail=0, gpu_coarsen=True)
+    host = AMGSolver(K, dense_tail=0, gpu_coarsen=False)
+    assert gpu.n_project() == host.n_project() >= 2
+    for l in range(host.n_project()):
+        for a, b in zip(gpu.projection(l), host.projection(l)):
+            assert np.array_equal(a, b), (case, l)
+        for a, b in zip(gpu.level_matrix(l + 1), host.level_matrix(l + 1)):
+            assert np.array_equal(a, b), (case, l)
+    rp, ci, va = K.download()
+    P, _ = O.project(O.CSR(rp, ci, va, (rp.shape[0] - 1,) * 2))
+    prp, pci, pva = gpu.projection(0)
+    assert np.array_equal(prp, P.rowptr) and np.array_equal(pci, P.cols) and np.array_equal(pva, P.vals)
+
+
 @pytest.mark.parametrize("name", golden_names())
 def test_vcycles_converge(ctx, name):
     from afepack_gb300.amg import AMGSolver
