@@ -99,6 +99,12 @@ SIGNATURES = {
     "afp_context_stream": [C.c_void_p, c_void_pp],
     "afp_space_create": [C.c_void_p, C.c_int, C.c_int, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                          C.c_void_p, c_void_pp],
+    "afp_space_create_numbered": [C.c_void_p, C.c_int, C.c_int, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
+                                  C.c_void_p, C.c_void_p],
+    "afp_space_info": [C.c_void_p, C.c_void_p, C.c_void_p],
+    "afp_space_download_dofs": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+    "afp_quadrature_points": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+    "afp_l2_discretize": [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int64, C.c_void_p],
     "afp_space_destroy": [C.c_void_p],
     "afp_assemble": [C.c_void_p, C.POINTER(AssembleOpts), c_void_pp, c_void_pp],
     "afp_matrix_create_csr": [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -16,6 +16,7 @@
 // [diagonal, ascending others] (SparsityPattern::compress, SparsityPattern.h:193-237).
 // The values pass walks the same incidence list in ascending cell order,
 // so no atomics are needed and the result is deterministic.
+#include <algorithm>
 #include <climits>
 
 #include "common.cuh"
@@ -32,6 +33,10 @@ struct afp_space {
   afp::DevBuf<int> inc_ptr;  // n_dof+1
   afp::DevBuf<int> inc;      // cell*nd + local, ascending per DOF
   int max_inc = 0;
+  // spaces numbered on the device (afp_space_create_numbered) also keep
+  // each DOF's boundary mark and interpolation point
+  afp::DevBuf<int> dof_bmark;
+  afp::DevBuf<double> dof_point;
 };
 
 namespace afp {
@@ -74,6 +79,96 @@ __global__ void k_sort_lists(const int* __restrict__ ptr, int* __restrict__ list
   }
 }
 
+// ---------------------------------------------------- DOF numbering
+// FEMSpace::buildDof (include/AFEPack/FEMSpace.templates.h:884-1003) numbers
+// the DOFs in the order the element loop first touches their geometries:
+// elements in order, inside an element the template's vertices, then its
+// edges.  A "touch" is slot s of element e, t = e*T + s (T = slots per
+// element, vertices first), so a geometry's DOF number is the number of
+// first touches before its own first touch: an exclusive scan over first-touch
+// flags.  The first touch of a vertex is the lowest (cell, local vertex) of
+// its incidence list; that of an edge (a, b) is the lowest cell holding both,
+// found by walking a's incidence list in ascending cell order.
+
+// template edges as local vertex pairs, in template order
+__constant__ int c_tri_edge[3][2] = {{1, 2}, {0, 2}, {0, 1}};
+__constant__ int c_tet_edge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {2, 3}, {1, 3}, {1, 2}};
+
+__device__ __forceinline__ void edge_verts(int dim, int j, int& a, int& b) {
+  if (dim == 2) {
+    a = c_tri_edge[j][0];
+    b = c_tri_edge[j][1];
+  } else {
+    a = c_tet_edge[j][0];
+    b = c_tet_edge[j][1];
+  }
+}
+
+// first[t] = flat touch index of the first touch of slot t's geometry
+__global__ void k_first_touch(int dim, int degree, int64_t n_cell, const int* __restrict__ cells,
+                              const int* __restrict__ vptr, const int* __restrict__ vinc, int* __restrict__ first,
+                              int* __restrict__ is_first) {
+  const int nv = dim + 1, ne = degree == 2 ? (dim == 2 ? 3 : 6) : 0, T = nv + ne;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_cell * T) return;
+  const int64_t e = t / T;
+  const int s = (int)(t - e * T);
+  int64_t f;
+  if (s < nv) {
+    const int v = cells[e * nv + s];
+    const int g = vinc[vptr[v]];  // lowest cell*nv + local of vertex v
+    f = (int64_t)(g / nv) * T + g % nv;
+  } else {
+    int la, lb;
+    edge_verts(dim, s - nv, la, lb);
+    const int a = cells[e * nv + la], b = cells[e * nv + lb];
+    f = t;
+    for (int q = vptr[a]; q < vptr[a + 1]; ++q) {
+      const int c = vinc[q] / nv;
+      if (c >= e) break;  // the cell itself holds the edge
+      int jb = -1;
+      for (int k = 0; k < nv; ++k)
+        if (cells[(int64_t)c * nv + k] == b) jb = k;
+      if (jb < 0) continue;
+      const int ja = vinc[q] % nv;
+      for (int j = 0; j < ne; ++j) {
+        int x, y;
+        edge_verts(dim, j, x, y);
+        if ((x == ja && y == jb) || (x == jb && y == ja)) f = (int64_t)c * T + nv + j;
+      }
+      break;
+    }
+  }
+  first[t] = (int)f;
+  is_first[t] = f == t ? 1 : 0;
+}
+
+__global__ void k_number_dofs(int dim, int degree, int64_t n_cell, const int* __restrict__ cells,
+                              const double* __restrict__ coords, const int* __restrict__ vmark,
+                              const int* __restrict__ first, const int* __restrict__ rank, int* __restrict__ elem_dof,
+                              int* __restrict__ dof_bmark, double* __restrict__ dof_point) {
+  const int nv = dim + 1, ne = degree == 2 ? (dim == 2 ? 3 : 6) : 0, T = nv + ne;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_cell * T) return;
+  const int d = rank[first[t]];
+  elem_dof[t] = d;
+  if (first[t] != t) return;
+  const int64_t e = t / T;
+  const int s = (int)(t - e * T);
+  if (s < nv) {
+    const int v = cells[e * nv + s];
+    dof_bmark[d] = (vmark != nullptr && vmark[v] != 0) ? 1 : 0;
+    for (int k = 0; k < dim; ++k) dof_point[(int64_t)d * dim + k] = coords[(int64_t)v * dim + k];
+  } else {
+    int la, lb;
+    edge_verts(dim, s - nv, la, lb);
+    const int a = cells[e * nv + la], b = cells[e * nv + lb];
+    dof_bmark[d] = (vmark != nullptr && (vmark[a] & vmark[b]) != 0) ? 1 : 0;
+    for (int k = 0; k < dim; ++k)
+      dof_point[(int64_t)d * dim + k] = 0.5 * (coords[(int64_t)a * dim + k] + coords[(int64_t)b * dim + k]);
+  }
+}
+
 __global__ void k_max_diff(const int* __restrict__ ptr, int64_t n, int* __restrict__ out) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int v = i < n ? ptr[i + 1] - ptr[i] : 0;
@@ -111,6 +206,66 @@ struct Elem {
   static constexpr int ND = DIM == 2 ? 3 * DEG : (DEG == 1 ? 4 : 10);
 };
 
+// Quadrature point l of a triangle: its global point p and the basis values
+// of triangle.{1,2}.bas_fun.c there (lam: barycentric coordinates, P2 only).
+template <int DEG>
+__device__ __forceinline__ void tri_values(const double (&gv)[3][2], double area, const double (&R)[3][2],
+                                           double larea, const QuadRule& q, int l, double (&p)[2], double (&lam)[3],
+                                           double* val) {
+  const double lp[2] = {q.p[l][0], q.p[l][1]};
+  const double l0 = area2(lp, R[1], R[2]) / larea;
+  const double l1 = area2(lp, R[2], R[0]) / larea;
+  const double l2 = area2(lp, R[0], R[1]) / larea;
+  p[0] = l0 * gv[0][0] + l1 * gv[1][0] + l2 * gv[2][0];
+  p[1] = l0 * gv[0][1] + l1 * gv[1][1] + l2 * gv[2][1];
+  if constexpr (DEG == 1) {
+    val[0] = area2(p, gv[1], gv[2]) / area;
+    val[1] = area2(gv[0], p, gv[2]) / area;
+    val[2] = area2(gv[0], gv[1], p) / area;
+  } else {
+    lam[0] = area2(p, gv[1], gv[2]) / area;
+    lam[1] = area2(p, gv[2], gv[0]) / area;
+    lam[2] = area2(p, gv[0], gv[1]) / area;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) val[k] = lam[k] * (2 * lam[k] - 1.0);
+    val[3] = 4.0 * lam[1] * lam[2];
+    val[4] = 4.0 * lam[0] * lam[2];
+    val[5] = 4.0 * lam[0] * lam[1];
+  }
+}
+
+// the same for a tetrahedron (tetrahedron.{1,2}.bas_fun.c); vol = det6 of the cell
+template <int DEG>
+__device__ __forceinline__ void tet_values(const double (&v)[4][3], double vol, const double (&R)[4][3], double lvol,
+                                           const QuadRule& q, int l, double (&p)[3], double (&lam)[4],
+                                           double* val) {
+  const double lp[3] = {q.p[l][0], q.p[l][1], q.p[l][2]};
+  const double l0 = det6(lp, R[1], R[2], R[3]) / 6. / lvol;
+  const double l1 = det6(R[0], lp, R[2], R[3]) / 6. / lvol;
+  const double l2 = det6(R[0], R[1], lp, R[3]) / 6. / lvol;
+  const double l3 = det6(R[0], R[1], R[2], lp) / 6. / lvol;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) p[d] = l0 * v[0][d] + l1 * v[1][d] + l2 * v[2][d] + l3 * v[3][d];
+  lam[0] = det6(p, v[1], v[2], v[3]) / vol;
+  lam[1] = det6(v[0], p, v[2], v[3]) / vol;
+  lam[2] = det6(v[0], v[1], p, v[3]) / vol;
+  lam[3] = det6(v[0], v[1], v[2], p) / vol;
+  if constexpr (DEG == 1) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) val[m] = lam[m];
+  } else {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) val[m] = lam[m] * (2 * lam[m] - 1);
+    // template edges 0:(0,1) 1:(0,2) 2:(0,3) 3:(2,3) 4:(1,3) 5:(1,2)
+    val[4] = 4.0 * lam[0] * lam[1];
+    val[5] = 4.0 * lam[0] * lam[2];
+    val[6] = 4.0 * lam[0] * lam[3];
+    val[7] = 4.0 * lam[2] * lam[3];
+    val[8] = 4.0 * lam[1] * lam[3];
+    val[9] = 4.0 * lam[1] * lam[2];
+  }
+}
+
 // Element matrix of one cell, reference arithmetic (see file comment).
 template <int DIM, int DEG, bool MASS>
 __global__ void __launch_bounds__(128) k_element_matrix(const double* __restrict__ coords, const int* __restrict__ cells,
@@ -143,31 +298,18 @@ __global__ void __launch_bounds__(128) k_element_matrix(const double* __restrict
     dx[1] = (gv[2][1] - gv[0][1]) / area; dy[1] = (gv[0][0] - gv[2][0]) / area;
     dx[2] = (gv[0][1] - gv[1][1]) / area; dy[2] = (gv[1][0] - gv[0][0]) / area;
     for (int l = 0; l < q.n; ++l) {
-      const double lp[2] = {q.p[l][0], q.p[l][1]};
-      const double l0 = area2(lp, R[1], R[2]) / larea;
-      const double l1 = area2(lp, R[2], R[0]) / larea;
-      const double l2 = area2(lp, R[0], R[1]) / larea;
-      const double p[2] = {l0 * gv[0][0] + l1 * gv[1][0] + l2 * gv[2][0], l0 * gv[0][1] + l1 * gv[1][1] + l2 * gv[2][1]};
+      double p[2], lam[3], val[ND], g[ND][2];
+      tri_values<DEG>(gv, area, R, larea, q, l, p, lam, val);
       const double Jxw = q.p[l][2] * jac * tmpl_volume;
-      double val[ND], g[ND][2];
       if constexpr (DEG == 1) {
-        val[0] = area2(p, gv[1], gv[2]) / area;
-        val[1] = area2(gv[0], p, gv[2]) / area;
-        val[2] = area2(gv[0], gv[1], p) / area;
 #pragma unroll
         for (int k = 0; k < 3; ++k) { g[k][0] = dx[k]; g[k][1] = dy[k]; }
       } else {
-        const double lam[3] = {area2(p, gv[1], gv[2]) / area, area2(p, gv[2], gv[0]) / area,
-                               area2(p, gv[0], gv[1]) / area};
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          val[k] = lam[k] * (2 * lam[k] - 1.0);
           g[k][0] = (4.0 * lam[k] - 1.0) * dx[k];
           g[k][1] = (4.0 * lam[k] - 1.0) * dy[k];
         }
-        val[3] = 4.0 * lam[1] * lam[2];
-        val[4] = 4.0 * lam[0] * lam[2];
-        val[5] = 4.0 * lam[0] * lam[1];
         g[3][0] = 4.0 * (lam[2] * dx[1] + lam[1] * dx[2]); g[3][1] = 4.0 * (lam[2] * dy[1] + lam[1] * dy[2]);
         g[4][0] = 4.0 * (lam[0] * dx[2] + lam[2] * dx[0]); g[4][1] = 4.0 * (lam[0] * dy[2] + lam[2] * dy[0]);
         g[5][0] = 4.0 * (lam[1] * dx[0] + lam[0] * dx[1]); g[5][1] = 4.0 * (lam[1] * dy[0] + lam[0] * dy[1]);
@@ -198,32 +340,19 @@ __global__ void __launch_bounds__(128) k_element_matrix(const double* __restrict
 #pragma unroll
       for (int n = 0; n < 3; ++n) gl[m][n] = co_det(v, m, n) / vol;
     for (int l = 0; l < q.n; ++l) {
-      const double lp[3] = {q.p[l][0], q.p[l][1], q.p[l][2]};
-      const double l0 = det6(lp, R[1], R[2], R[3]) / 6. / lvol;
-      const double l1 = det6(R[0], lp, R[2], R[3]) / 6. / lvol;
-      const double l2 = det6(R[0], R[1], lp, R[3]) / 6. / lvol;
-      const double l3 = det6(R[0], R[1], R[2], lp) / 6. / lvol;
-      double p[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) p[d] = l0 * v[0][d] + l1 * v[1][d] + l2 * v[2][d] + l3 * v[3][d];
+      double p[3], lam[4], val[ND], g[ND][3];
+      tet_values<DEG>(v, vol, R, lvol, q, l, p, lam, val);
       const double Jxw = q.p[l][3] * jac * tmpl_volume;
-      const double lam[4] = {det6(p, v[1], v[2], v[3]) / vol, det6(v[0], p, v[2], v[3]) / vol,
-                             det6(v[0], v[1], p, v[3]) / vol, det6(v[0], v[1], v[2], p) / vol};
-      double val[ND], g[ND][3];
       if constexpr (DEG == 1) {
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          val[m] = lam[m];
+        for (int m = 0; m < 4; ++m)
 #pragma unroll
           for (int n = 0; n < 3; ++n) g[m][n] = gl[m][n];
-        }
       } else {
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          val[m] = lam[m] * (2 * lam[m] - 1);
+        for (int m = 0; m < 4; ++m)
 #pragma unroll
           for (int n = 0; n < 3; ++n) g[m][n] = gl[m][n] * (4. * lam[m] - 1.);
-        }
         // template edges 0:(0,1) 1:(0,2) 2:(0,3) 3:(2,3) 4:(1,3) 5:(1,2);
         // the gradient of 4 l_a l_b is 4*(gl[first]*l[la] + gl[second]*l[lb])
         // with the operand order of the plugin function attached to the edge.
@@ -231,12 +360,6 @@ __global__ void __launch_bounds__(128) k_element_matrix(const double* __restrict
         constexpr int second[6] = {0, 0, 0, 3, 3, 2};
         constexpr int la[6] = {0, 0, 0, 3, 3, 2};
         constexpr int lb[6] = {1, 2, 3, 2, 1, 1};
-        val[4] = 4.0 * lam[0] * lam[1];
-        val[5] = 4.0 * lam[0] * lam[2];
-        val[6] = 4.0 * lam[0] * lam[3];
-        val[7] = 4.0 * lam[2] * lam[3];
-        val[8] = 4.0 * lam[1] * lam[3];
-        val[9] = 4.0 * lam[1] * lam[2];
 #pragma unroll
         for (int t = 0; t < 6; ++t)
 #pragma unroll
@@ -266,6 +389,99 @@ __global__ void __launch_bounds__(128) k_element_matrix(const double* __restrict
   double* o = out + e * (ND * ND);
 #pragma unroll
   for (int t = 0; t < ND * ND; ++t) o[t] = K[t];
+}
+
+// ---------------------------------------------------- L2Discretize
+// Operator::L2Discretize (include/AFEPack/Operator.discretize.templates.h)
+// adds Jxw f(q_l) phi_j(q_l) into f1[dof_j] element by element, point by
+// point.  Each DOF therefore receives its terms in (cell, point) order; the
+// terms are formed per cell here and summed per DOF in that order by
+// k_gather_rhs, which gives the reference's sums bit for bit.
+enum RhsSource { SRC_POINT_VALUES = 0, SRC_FEM_FUNCTION = 1, SRC_GAUSSIANS = 2 };
+
+template <int DIM, int DEG, int SRC>
+__global__ void __launch_bounds__(128) k_element_rhs(const double* __restrict__ coords, const int* __restrict__ cells,
+                                                     const int* __restrict__ elem_dof, int64_t c0, int64_t c1,
+                                                     QuadRule q, const double* __restrict__ data, int n_gauss,
+                                                     double* __restrict__ terms, double* __restrict__ points) {
+  constexpr int NV = Elem<DIM, DEG>::NV, ND = Elem<DIM, DEG>::ND;
+  const int64_t e = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= c1) return;
+  double v[4][3] = {{0}};
+#pragma unroll
+  for (int a = 0; a < NV; ++a) {
+    const int vi = cells[e * NV + a];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) v[a][d] = coords[(int64_t)vi * DIM + d];
+  }
+  for (int l = 0; l < q.n; ++l) {
+    double p[DIM], val[ND], Jxw;
+    if constexpr (DIM == 2) {
+      const double R[3][2] = {{0.0, 0.0}, {1.0, 0.0}, {0.0, 1.0}};
+      const double larea = area2(R[0], R[1], R[2]);
+      const double tmpl_volume = .5 * area2(R[0], R[1], R[2]);
+      const double gv[3][2] = {{v[0][0], v[0][1]}, {v[1][0], v[1][1]}, {v[2][0], v[2][1]}};
+      const double garea = area2(gv[0], gv[1], gv[2]);
+      double lam[3];
+      tri_values<DEG>(gv, garea, R, larea, q, l, p, lam, val);
+      Jxw = q.p[l][2] * (garea / larea) * tmpl_volume;
+    } else {
+      const double R[4][3] = {{0.0, 0.0, 0.0}, {1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}};
+      const double lvol = det6(R[0], R[1], R[2], R[3]) / 6.;
+      const double tmpl_volume = det6(R[0], R[1], R[2], R[3]) / 6.;
+      const double jac = (det6(v[0], v[1], v[2], v[3]) / 6.) / lvol;
+      double lam[4];
+      tet_values<DEG>(v, det6(v[0], v[1], v[2], v[3]), R, lvol, q, l, p, lam, val);
+      Jxw = q.p[l][3] * jac * tmpl_volume;
+    }
+    const int64_t ql = (e - c0) * q.n + l;
+    if (points != nullptr) {
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) points[(e * q.n + l) * DIM + d] = p[d];
+    }
+    if (terms == nullptr) continue;
+    double f = 0;
+    if constexpr (SRC == SRC_POINT_VALUES) {
+      f = data[e * q.n + l];
+    } else if constexpr (SRC == SRC_FEM_FUNCTION) {
+      // FEMFunction::value (include/AFEPack/FEMSpace.templates.h:1087-1100)
+#pragma unroll
+      for (int j = 0; j < ND; ++j) f += data[elem_dof[e * ND + j]] * val[j];
+    } else {
+      // sum of amp * exp(-|p - c|^2 / (2 s^2)); data: [c (DIM), s, amp] per Gaussian
+      for (int g = 0; g < n_gauss; ++g) {
+        const double* c = data + g * (DIM + 2);
+        double r2 = 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const double t = p[d] - c[d];
+          r2 += t * t;
+        }
+        const double s = c[DIM];
+        f += c[DIM + 1] * exp(-r2 / (2.0 * s * s));
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < ND; ++j) terms[ql * ND + j] = Jxw * f * val[j];
+  }
+}
+
+// f1[i] += the terms of the cells [c0, c1) around DOF i, ascending cell, then point
+__global__ void k_gather_rhs(int64_t n_dof, const int* __restrict__ inc_ptr, const int* __restrict__ inc, int nd,
+                             int nq, int64_t c0, int64_t c1, const double* __restrict__ terms,
+                             double* __restrict__ f1) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_dof) return;
+  double acc = f1[i];
+  for (int p = inc_ptr[i]; p < inc_ptr[i + 1]; ++p) {
+    const int qd = inc[p];
+    const int64_t c = qd / nd;
+    if (c < c0) continue;
+    if (c >= c1) break;
+    const double* t = terms + ((c - c0) * nq) * nd + qd % nd;
+    for (int l = 0; l < nq; ++l) acc += t[(int64_t)l * nd];
+  }
+  f1[i] = acc;
 }
 
 // ------------------------------------------------------------ pattern
@@ -456,6 +672,34 @@ void element_matrices(const afp_space* sp, int acc, const double* coef, bool mas
   else element_matrices<3, 2>(sp, q, coef, mass, out);
 }
 
+template <int DIM, int DEG>
+void element_rhs(const afp_space* sp, int src, int64_t c0, int64_t c1, const QuadRule& q, const double* data,
+                 int n_gauss, double* terms, double* points) {
+  const afp_context* ctx = sp->ctx;
+  const unsigned grid = grid_for(c1 - c0, 128);
+  const double* co = sp->coords.get();
+  const int* ce = sp->cells.get();
+  const int* ed = sp->elem_dof.get();
+  if (src == SRC_POINT_VALUES)
+    k_element_rhs<DIM, DEG, SRC_POINT_VALUES><<<grid, 128, 0, ctx->stream>>>(co, ce, ed, c0, c1, q, data, n_gauss,
+                                                                             terms, points);
+  else if (src == SRC_FEM_FUNCTION)
+    k_element_rhs<DIM, DEG, SRC_FEM_FUNCTION><<<grid, 128, 0, ctx->stream>>>(co, ce, ed, c0, c1, q, data, n_gauss,
+                                                                             terms, points);
+  else
+    k_element_rhs<DIM, DEG, SRC_GAUSSIANS><<<grid, 128, 0, ctx->stream>>>(co, ce, ed, c0, c1, q, data, n_gauss,
+                                                                          terms, points);
+  check_launch(ctx, "element right-hand sides");
+}
+
+void element_rhs(const afp_space* sp, int src, int64_t c0, int64_t c1, const QuadRule& q, const double* data,
+                 int n_gauss, double* terms, double* points) {
+  if (sp->dim == 2 && sp->degree == 1) element_rhs<2, 1>(sp, src, c0, c1, q, data, n_gauss, terms, points);
+  else if (sp->dim == 2 && sp->degree == 2) element_rhs<2, 2>(sp, src, c0, c1, q, data, n_gauss, terms, points);
+  else if (sp->dim == 3 && sp->degree == 1) element_rhs<3, 1>(sp, src, c0, c1, q, data, n_gauss, terms, points);
+  else element_rhs<3, 2>(sp, src, c0, c1, q, data, n_gauss, terms, points);
+}
+
 template <int ND>
 void build_pattern_nd(const afp_space* sp, Pattern& pat) {
   const afp_context* ctx = sp->ctx;
@@ -528,65 +772,203 @@ using namespace afp;
 
 extern "C" {
 
+namespace {
+
+// checks the index arrays and builds the DOF -> (cell, local) incidence of a
+// space whose cells and elem_dof are on the device
+void finish_space(afp_space* sp) {
+  afp_context* ctx = sp->ctx;
+  const int64_t n_cell = sp->n_cell, n_dof = sp->n_dof;
+  DevBuf<int> bad(ctx, 2);
+  bad.zero();
+  const int64_t ncd = n_cell * sp->nd, ncv = n_cell * sp->nv;
+  k_check_range<<<grid_for(ncv, BLOCK), BLOCK, 0, ctx->stream>>>(sp->cells.get(), ncv, sp->n_vertex, bad.get());
+  check_launch(ctx, "check cells");
+  k_check_range<<<grid_for(ncd, BLOCK), BLOCK, 0, ctx->stream>>>(sp->elem_dof.get(), ncd, n_dof, bad.get() + 1);
+  check_launch(ctx, "check dofs");
+  int hb[2];
+  bad.download(hb, 2);
+  sync(ctx);
+  AFP_REQUIRE(!hb[0], AFP_ERR_INVALID, "cell vertex index out of range");
+  AFP_REQUIRE(!hb[1], AFP_ERR_INVALID, "element DOF index out of range");
+  // DOF -> (cell, local) incidence, ascending cell order per DOF
+  DevBuf<int> cnt(ctx, n_dof);
+  cnt.zero();
+  k_count<<<grid_for(ncd, BLOCK), BLOCK, 0, ctx->stream>>>(sp->elem_dof.get(), ncd, cnt.get());
+  check_launch(ctx, "incidence count");
+  sp->inc_ptr.alloc(ctx, n_dof + 1);
+  exclusive_scan(ctx, cnt.get(), sp->inc_ptr.get(), n_dof);
+  sp->inc.alloc(ctx, ncd);
+  cnt.zero();
+  k_fill_incidence<<<grid_for(ncd, BLOCK), BLOCK, 0, ctx->stream>>>(sp->elem_dof.get(), ncd, sp->inc_ptr.get(),
+                                                                    cnt.get(), sp->inc.get());
+  check_launch(ctx, "incidence fill");
+  k_sort_lists<<<grid_for(n_dof, BLOCK), BLOCK, 0, ctx->stream>>>(sp->inc_ptr.get(), sp->inc.get(), n_dof);
+  check_launch(ctx, "incidence sort");
+  DevBuf<int> mx(ctx, 1);
+  mx.zero();
+  k_max_diff<<<grid_for(n_dof, BLOCK), BLOCK, 0, ctx->stream>>>(sp->inc_ptr.get(), n_dof, mx.get());
+  check_launch(ctx, "max incidence");
+  mx.download(&sp->max_inc, 1);
+  sync(ctx);
+}
+
+std::unique_ptr<afp_space> new_space(afp_context* ctx, int dim, int degree, int64_t n_vertex, const double* coords,
+                                     int64_t n_cell, const int32_t* cells) {
+  AFP_REQUIRE((dim == 2 || dim == 3) && (degree == 1 || degree == 2), AFP_ERR_UNSUPPORTED,
+              "only P1/P2 on triangles and tetrahedra");
+  AFP_REQUIRE(n_vertex > 0 && n_cell > 0, AFP_ERR_INVALID, "empty mesh");
+  auto sp = std::make_unique<afp_space>();
+  sp->ctx = ctx;
+  sp->dim = dim;
+  sp->degree = degree;
+  sp->nv = dim + 1;
+  sp->nd = dim == 2 ? 3 * degree : (degree == 1 ? 4 : 10);
+  sp->n_vertex = n_vertex;
+  sp->n_cell = n_cell;
+  AFP_REQUIRE(n_cell * sp->nd < INT32_MAX, AFP_ERR_UNSUPPORTED, "more than 2^31 cell DOFs");
+  sp->coords.alloc(ctx, n_vertex * dim);
+  sp->cells.alloc(ctx, n_cell * sp->nv);
+  sp->coords.upload(coords, n_vertex * dim);
+  sp->cells.upload(cells, n_cell * sp->nv);
+  return sp;
+}
+
+}  // namespace
+
 afp_status afp_space_create(afp_context* ctx, int dim, int degree, int64_t n_vertex, const double* coords,
                             int64_t n_cell, const int32_t* cells, int64_t n_dof, const int32_t* elem_dof,
                             afp_space** out) {
   return guarded([&] {
     AFP_REQUIRE(ctx && coords && cells && elem_dof && out, AFP_ERR_INVALID, "null argument");
-    AFP_REQUIRE((dim == 2 || dim == 3) && (degree == 1 || degree == 2), AFP_ERR_UNSUPPORTED,
-                "only P1/P2 on triangles and tetrahedra");
-    AFP_REQUIRE(n_vertex > 0 && n_cell > 0 && n_dof > 0, AFP_ERR_INVALID, "empty mesh");
+    AFP_REQUIRE(n_dof > 0, AFP_ERR_INVALID, "empty mesh");
     bind(ctx);
-    auto sp = std::make_unique<afp_space>();
-    sp->ctx = ctx;
-    sp->dim = dim;
-    sp->degree = degree;
-    sp->nv = dim + 1;
-    sp->nd = dim == 2 ? 3 * degree : (degree == 1 ? 4 : 10);
-    sp->n_vertex = n_vertex;
-    sp->n_cell = n_cell;
+    auto sp = new_space(ctx, dim, degree, n_vertex, coords, n_cell, cells);
     sp->n_dof = n_dof;
-    AFP_REQUIRE(n_cell * sp->nd < INT32_MAX, AFP_ERR_UNSUPPORTED, "more than 2^31 cell DOFs");
-    sp->coords.alloc(ctx, n_vertex * dim);
-    sp->cells.alloc(ctx, n_cell * sp->nv);
     sp->elem_dof.alloc(ctx, n_cell * sp->nd);
-    sp->coords.upload(coords, n_vertex * dim);
-    sp->cells.upload(cells, n_cell * sp->nv);
     sp->elem_dof.upload(elem_dof, n_cell * sp->nd);
-    // validate indices before any kernel trusts them
-    DevBuf<int> bad(ctx, 2);
+    finish_space(sp.get());
+    *out = sp.release();
+  });
+}
+
+afp_status afp_space_create_numbered(afp_context* ctx, int dim, int degree, int64_t n_vertex, const double* coords,
+                                     int64_t n_cell, const int32_t* cells, const int32_t* vertex_bmark,
+                                     afp_space** out) {
+  return guarded([&] {
+    AFP_REQUIRE(ctx && coords && cells && out, AFP_ERR_INVALID, "null argument");
+    bind(ctx);
+    auto sp = new_space(ctx, dim, degree, n_vertex, coords, n_cell, cells);
+    const int64_t ncv = n_cell * sp->nv, T = sp->nd, nt = n_cell * T;
+    DevBuf<int> bad(ctx, 1);
     bad.zero();
-    const int64_t ncd = n_cell * sp->nd, ncv = n_cell * sp->nv;
     k_check_range<<<grid_for(ncv, BLOCK), BLOCK, 0, ctx->stream>>>(sp->cells.get(), ncv, n_vertex, bad.get());
     check_launch(ctx, "check cells");
-    k_check_range<<<grid_for(ncd, BLOCK), BLOCK, 0, ctx->stream>>>(sp->elem_dof.get(), ncd, n_dof, bad.get() + 1);
-    check_launch(ctx, "check dofs");
-    int hb[2];
-    bad.download(hb, 2);
+    int hb = 0;
+    bad.download(&hb, 1);
     sync(ctx);
-    AFP_REQUIRE(!hb[0], AFP_ERR_INVALID, "cell vertex index out of range");
-    AFP_REQUIRE(!hb[1], AFP_ERR_INVALID, "element DOF index out of range");
-    // DOF -> (cell, local) incidence, ascending cell order per DOF
-    DevBuf<int> cnt(ctx, n_dof);
-    cnt.zero();
-    k_count<<<grid_for(ncd, BLOCK), BLOCK, 0, ctx->stream>>>(sp->elem_dof.get(), ncd, cnt.get());
-    check_launch(ctx, "incidence count");
-    sp->inc_ptr.alloc(ctx, n_dof + 1);
-    exclusive_scan(ctx, cnt.get(), sp->inc_ptr.get(), n_dof);
-    sp->inc.alloc(ctx, ncd);
-    cnt.zero();
-    k_fill_incidence<<<grid_for(ncd, BLOCK), BLOCK, 0, ctx->stream>>>(sp->elem_dof.get(), ncd, sp->inc_ptr.get(),
-                                                                      cnt.get(), sp->inc.get());
-    check_launch(ctx, "incidence fill");
-    k_sort_lists<<<grid_for(n_dof, BLOCK), BLOCK, 0, ctx->stream>>>(sp->inc_ptr.get(), sp->inc.get(), n_dof);
-    check_launch(ctx, "incidence sort");
-    DevBuf<int> mx(ctx, 1);
-    mx.zero();
-    k_max_diff<<<grid_for(n_dof, BLOCK), BLOCK, 0, ctx->stream>>>(sp->inc_ptr.get(), n_dof, mx.get());
-    check_launch(ctx, "max incidence");
-    mx.download(&sp->max_inc, 1);
-    sync(ctx);
+    AFP_REQUIRE(!hb, AFP_ERR_INVALID, "cell vertex index out of range");
+    // vertex -> (cell, local vertex) incidence, ascending cell order
+    DevBuf<int> vcnt(ctx, n_vertex), vptr(ctx, n_vertex + 1), vinc(ctx, ncv);
+    vcnt.zero();
+    k_count<<<grid_for(ncv, BLOCK), BLOCK, 0, ctx->stream>>>(sp->cells.get(), ncv, vcnt.get());
+    exclusive_scan(ctx, vcnt.get(), vptr.get(), n_vertex);
+    vcnt.zero();
+    k_fill_incidence<<<grid_for(ncv, BLOCK), BLOCK, 0, ctx->stream>>>(sp->cells.get(), ncv, vptr.get(), vcnt.get(),
+                                                                      vinc.get());
+    k_sort_lists<<<grid_for(n_vertex, BLOCK), BLOCK, 0, ctx->stream>>>(vptr.get(), vinc.get(), n_vertex);
+    check_launch(ctx, "vertex incidence");
+    DevBuf<int> first(ctx, nt), is_first(ctx, nt), rank(ctx, nt + 1);
+    k_first_touch<<<grid_for(nt, BLOCK), BLOCK, 0, ctx->stream>>>(dim, degree, n_cell, sp->cells.get(), vptr.get(),
+                                                                  vinc.get(), first.get(), is_first.get());
+    check_launch(ctx, "first touch");
+    sp->n_dof = exclusive_scan(ctx, is_first.get(), rank.get(), nt);
+    DevBuf<int> vmark;
+    if (vertex_bmark) {
+      vmark.alloc(ctx, n_vertex);
+      vmark.upload(vertex_bmark, n_vertex);
+    }
+    sp->elem_dof.alloc(ctx, nt);
+    sp->dof_bmark.alloc(ctx, sp->n_dof);
+    sp->dof_point.alloc(ctx, sp->n_dof * dim);
+    k_number_dofs<<<grid_for(nt, BLOCK), BLOCK, 0, ctx->stream>>>(
+        dim, degree, n_cell, sp->cells.get(), sp->coords.get(), vertex_bmark ? vmark.get() : nullptr, first.get(),
+        rank.get(), sp->elem_dof.get(), sp->dof_bmark.get(), sp->dof_point.get());
+    check_launch(ctx, "DOF numbering");
+    finish_space(sp.get());
     *out = sp.release();
+  });
+}
+
+afp_status afp_space_info(const afp_space* sp, int64_t* n_dof, int* nd) {
+  return guarded([&] {
+    AFP_REQUIRE(sp, AFP_ERR_INVALID, "null argument");
+    if (n_dof) *n_dof = sp->n_dof;
+    if (nd) *nd = sp->nd;
+  });
+}
+
+afp_status afp_space_download_dofs(const afp_space* sp, int32_t* elem_dof, int32_t* dof_bmark, double* dof_point) {
+  return guarded([&] {
+    AFP_REQUIRE(sp, AFP_ERR_INVALID, "null argument");
+    AFP_REQUIRE((!dof_bmark && !dof_point) || sp->dof_bmark.size() > 0, AFP_ERR_INVALID,
+                "boundary marks and points exist only for spaces numbered by afp_space_create_numbered");
+    bind(sp->ctx);
+    if (elem_dof) sp->elem_dof.download(elem_dof, sp->n_cell * sp->nd);
+    if (dof_bmark) sp->dof_bmark.download(dof_bmark, sp->n_dof);
+    if (dof_point) sp->dof_point.download(dof_point, sp->n_dof * sp->dim);
+    sync(sp->ctx);
+  });
+}
+
+afp_status afp_quadrature_points(afp_space* sp, int acc, int* n_q, double* points) {
+  return guarded([&] {
+    AFP_REQUIRE(sp, AFP_ERR_INVALID, "null argument");
+    bind(sp->ctx);
+    const QuadRule q = make_rule(sp->dim, acc);
+    if (n_q) *n_q = q.n;
+    if (!points) return;
+    DevBuf<double> pts(sp->ctx, sp->n_cell * q.n * sp->dim);
+    element_rhs(sp, SRC_POINT_VALUES, 0, sp->n_cell, q, nullptr, 0, nullptr, pts.get());
+    pts.download(points, sp->n_cell * q.n * sp->dim);
+    sync(sp->ctx);
+  });
+}
+
+afp_status afp_l2_discretize(afp_space* sp, int acc, int source, const double* data, int64_t n_data, double* f1) {
+  return guarded([&] {
+    AFP_REQUIRE(sp && data && f1, AFP_ERR_INVALID, "null argument");
+    bind(sp->ctx);
+    afp_context* ctx = sp->ctx;
+    const QuadRule q = make_rule(sp->dim, acc);
+    int n_gauss = 0;
+    if (source == SRC_POINT_VALUES)
+      AFP_REQUIRE(n_data == sp->n_cell * q.n, AFP_ERR_INVALID, "point values: n_data must be n_cell * n_q");
+    else if (source == SRC_FEM_FUNCTION)
+      AFP_REQUIRE(n_data == sp->n_dof, AFP_ERR_INVALID, "FEM function: n_data must be n_dof");
+    else if (source == SRC_GAUSSIANS) {
+      AFP_REQUIRE(n_data >= 0 && n_data % (sp->dim + 2) == 0, AFP_ERR_INVALID,
+                  "Gaussians: n_data must be a multiple of dim + 2");
+      n_gauss = (int)(n_data / (sp->dim + 2));
+    } else
+      fail(AFP_ERR_INVALID, "unknown source");
+    DevBuf<double> d(ctx, n_data > 0 ? n_data : 1), out(ctx, sp->n_dof);
+    d.upload(data, n_data);
+    out.zero();
+    // terms of at most ~256 MB at a time; cells in ascending chunks keep the per-DOF order
+    const int64_t per_cell = (int64_t)q.n * sp->nd;
+    const int64_t chunk = std::max<int64_t>(1, ((int64_t)256 << 20) / 8 / per_cell);
+    DevBuf<double> terms(ctx, std::min(chunk, sp->n_cell) * per_cell);
+    for (int64_t c0 = 0; c0 < sp->n_cell; c0 += chunk) {
+      const int64_t c1 = std::min(sp->n_cell, c0 + chunk);
+      element_rhs(sp, source, c0, c1, q, d.get(), n_gauss, terms.get(), nullptr);
+      k_gather_rhs<<<grid_for(sp->n_dof, BLOCK), BLOCK, 0, ctx->stream>>>(sp->n_dof, sp->inc_ptr.get(),
+                                                                          sp->inc.get(), sp->nd, q.n, c0, c1,
+                                                                          terms.get(), out.get());
+      check_launch(ctx, "right-hand side gather");
+    }
+    out.download(f1, sp->n_dof);
+    sync(ctx);
   });
 }
 

@@ -134,7 +134,7 @@ class Space:
     def __init__(self, ctx: Context, host: HostSpace):
         self.ctx = ctx
         self.host = host
-        mesh = host.mesh
+        self.mesh = mesh = host.mesh
         coords = np.ascontiguousarray(mesh.coords, dtype=np.float64)
         cells = np.ascontiguousarray(mesh.cells, dtype=np.int32)
         ed = np.ascontiguousarray(host.elem_dof, dtype=np.int32)
@@ -143,8 +143,40 @@ class Space:
                N.ptr(cells), host.n_dof, N.ptr(ed), C.byref(h))
         self.handle = h
 
+    @classmethod
+    def numbered(cls, ctx: Context, mesh, degree: int) -> "Space":
+        """FEMSpace::buildDof on the device: the DOF map, boundary marks and
+        interpolation points computed from the mesh alone."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.host = None
+        coords = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+        cells = np.ascontiguousarray(mesh.cells, dtype=np.int32)
+        bm = np.ascontiguousarray(mesh.bmask, dtype=np.int32)
+        h = C.c_void_p()
+        N.call("afp_space_create_numbered", ctx.handle, mesh.dim, degree, mesh.n_vertex, N.ptr(coords), mesh.n_cell,
+               N.ptr(cells), N.ptr(bm), C.byref(h))
+        self.handle = h
+        self.mesh = mesh
+        return self
+
+    def dofs(self):
+        """(elem_dof [n_cell, nd], dof_bmark [n_dof], dof_point [n_dof, dim]) of a numbered space."""
+        n, nd = C.c_int64(), C.c_int()
+        N.call("afp_space_info", self.handle, C.byref(n), C.byref(nd))
+        mesh = self.mesh
+        ed = np.empty((mesh.n_cell, nd.value), dtype=np.int32)
+        bm = np.empty(n.value, dtype=np.int32)
+        pt = np.empty((n.value, mesh.dim))
+        N.call("afp_space_download_dofs", self.handle, N.ptr(ed), N.ptr(bm), N.ptr(pt))
+        return ed, bm, pt
+
     @property
     def n_dof(self):
+        if self.host is None:
+            n = C.c_int64()
+            N.call("afp_space_info", self.handle, C.byref(n), None)
+            return n.value
         return self.host.n_dof
 
     def close(self):
@@ -172,12 +204,52 @@ def assemble(space: Space, acc_stiff: int, acc_mass: int | None = None, coef=Non
     return km, mm
 
 
+SOURCE_POINT_VALUES, SOURCE_FEM_FUNCTION, SOURCE_GAUSSIANS = 0, 1, 2
+
+
+def quadrature_points(space: Space, acc: int) -> np.ndarray:
+    """[n_cell, n_q, dim] global quadrature points of the rule of accuracy acc."""
+    nq = C.c_int()
+    N.call("afp_quadrature_points", space.handle, acc, C.byref(nq), None)
+    pts = np.empty((space.mesh.n_cell, nq.value, space.mesh.dim))
+    N.call("afp_quadrature_points", space.handle, acc, C.byref(nq), N.ptr(pts))
+    return pts
+
+
+class Gaussians:
+    """f(x) = sum_g amp_g exp(-|x - c_g|^2 / (2 s_g^2)), evaluated on the device."""
+
+    def __init__(self, centres, widths, amps=None):
+        centres = np.atleast_2d(np.asarray(centres, dtype=np.float64))
+        widths = np.asarray(widths, dtype=np.float64).reshape(-1, 1)
+        amps = np.ones_like(widths) if amps is None else np.asarray(amps, dtype=np.float64).reshape(-1, 1)
+        self.data = np.ascontiguousarray(np.concatenate([centres, widths, amps], axis=1))
+
+
+def L2Discretize(f, space: Space, acc: int) -> np.ndarray:
+    """Operator::L2Discretize(f, fem_space, f1, algebric_accuracy) on the GPU.
+
+    f: a callable of points [..., dim] (evaluated on the host at the device's
+    quadrature points, as the reference evaluates its function pointer), the
+    DOF values of a FEM function on `space`, or `Gaussians` (evaluated on the
+    device)."""
+    if isinstance(f, Gaussians):
+        src, data = SOURCE_GAUSSIANS, f.data
+    elif callable(f):
+        src, data = SOURCE_POINT_VALUES, np.ascontiguousarray(f(quadrature_points(space, acc)), dtype=np.float64)
+    else:
+        src, data = SOURCE_FEM_FUNCTION, np.ascontiguousarray(f, dtype=np.float64)
+    out = np.empty(space.n_dof)
+    N.call("afp_l2_discretize", space.handle, acc, src, N.ptr(data), data.size, N.ptr(out))
+    return out
+
+
 class StiffMatrix:
     """StiffMatrix<DIM,double>(fem_space): set algebricAccuracy, then build()."""
 
     def __init__(self, space: Space, coef=None):
         self.space = space
-        self.algebricAccuracy = 2 if space.host.mesh.dim == 3 else 4
+        self.algebricAccuracy = 2 if space.mesh.dim == 3 else 4
         self.coef = coef
         self.matrix: SparseMatrix | None = None
 

@@ -78,6 +78,23 @@ afp_status afp_context_launch_count(const afp_context *ctx, int64_t *count);
 afp_status afp_space_create(afp_context *ctx, int dim, int degree, int64_t n_vertex,
                             const double *coords, int64_t n_cell, const int32_t *cells,
                             int64_t n_dof, const int32_t *elem_dof, afp_space **out);
+/* FEMSpace::buildDof on the device (include/AFEPack/FEMSpace.templates.h:884-1003):
+ * the same space with the DOFs numbered as AFEPack numbers them -- elements
+ * in order, inside an element the template's vertices, then (P2) its edges,
+ * each geometry getting the next numbers the first time it is touched.
+ * Edges are identified by their vertex pairs.  vertex_bmark [n_vertex]
+ * (NULL: no boundary) gives each vertex a bit mask of the boundary pieces it
+ * lies on; a vertex DOF is on the boundary when its mask is nonzero, an edge
+ * DOF when its two vertices' masks share a bit. */
+afp_status afp_space_create_numbered(afp_context *ctx, int dim, int degree, int64_t n_vertex,
+                                     const double *coords, int64_t n_cell, const int32_t *cells,
+                                     const int32_t *vertex_bmark, afp_space **out);
+afp_status afp_space_info(const afp_space *sp, int64_t *n_dof, int *nd);
+/* elem_dof [n_cell*nd]; dof_bmark [n_dof] (1 on the boundary) and dof_point
+ * [n_dof*dim] (interpolation points) for spaces from
+ * afp_space_create_numbered; any pointer may be NULL. */
+afp_status afp_space_download_dofs(const afp_space *sp, int32_t *elem_dof, int32_t *dof_bmark,
+                                   double *dof_point);
 afp_status afp_space_destroy(afp_space *sp);
 
 /* ------------------------------------------------------------ assembly */
@@ -124,6 +141,31 @@ afp_status afp_matrix_vmult(afp_matrix *a, const double *x, double *y);
 #define AFP_NOALLOC_MAX_ENTRIES (1 << 21)
 afp_status afp_matrix_vmult_noalloc(afp_matrix *a, const double *x, double *y);
 afp_status afp_matrix_destroy(afp_matrix *a);
+
+/* Operator::L2Discretize(f, fem_space, f1, algebric_accuracy)
+ * (include/AFEPack/Operator.discretize.templates.h): f1_i = the sum, over
+ * the cells around DOF i and their quadrature points, of Jxw f(q) phi_i(q),
+ * added in the reference's order (bitwise its result for the first two
+ * sources).  source selects what f is:
+ *   AFP_SOURCE_POINT_VALUES  data = f at the quadrature points of
+ *       afp_quadrature_points, [n_cell*n_q] (the reference's function-pointer
+ *       form evaluates f at exactly these points, lines 151-183);
+ *   AFP_SOURCE_FEM_FUNCTION  data = a FEM function's DOF values [n_dof]
+ *       (L2Discretize(const FEMFunction&, f1, acc), lines 18-47);
+ *   AFP_SOURCE_GAUSSIANS     data = [centre (dim), width s, amplitude a] per
+ *       Gaussian: f = sum of a exp(-|x - c|^2 / (2 s^2)), evaluated on the
+ *       device (the CUDA exp, within an ulp of the host's).
+ * data and f1 may be host or device memory. */
+typedef enum afp_source {
+  AFP_SOURCE_POINT_VALUES = 0,
+  AFP_SOURCE_FEM_FUNCTION = 1,
+  AFP_SOURCE_GAUSSIANS = 2
+} afp_source;
+/* the global quadrature points [n_cell*n_q*dim] of the rule of accuracy acc
+ * (points may be NULL to query n_q) */
+afp_status afp_quadrature_points(afp_space *sp, int acc, int *n_q, double *points);
+afp_status afp_l2_discretize(afp_space *sp, int acc, int source, const double *data, int64_t n_data,
+                             double *f1);
 
 /* BoundaryConditionAdmin::apply(A, u, f, preserve_symmetry)
  * (include/AFEPack/FEMSpace.templates.h:1338-1366): for every DOF i with

@@ -321,6 +321,73 @@ int orc_assemble(int dim, int degree, const double *coords, int64_t n_cell, cons
   return 0;
 }
 
+/* the global point, Jxw and basis values of quadrature point l of cell vx */
+static void quad_point(int dim, int degree, const double *vx, const double *lp, double *gp, double *Jxw,
+                       double *val) {
+  double tv[4][3] = {{0}}, jac, grad[10][3];
+  for (int a = 0; a <= dim; ++a)
+    for (int d = 0; d < dim; ++d) tv[a][d] = vx[a * dim + d];
+  double tmpl_volume = dim == 2 ? .5 * area2(TRI_REF[0], TRI_REF[1], TRI_REF[2])
+                                : det6(TET_REF[0], TET_REF[1], TET_REF[2], TET_REF[3]) / 6.;
+  if (dim == 2) {
+    double gv[3][2] = {{tv[0][0], tv[0][1]}, {tv[1][0], tv[1][1]}, {tv[2][0], tv[2][1]}};
+    tri_l2g(lp, gv, gp, &jac);
+    tri_basis(degree, gv, gp, val, grad);
+  } else {
+    tet_l2g(lp, (const double(*)[3])tv, gp, &jac);
+    tet_basis(degree, (const double(*)[3])tv, gp, val, grad);
+  }
+  *Jxw = lp[dim] * jac * tmpl_volume;
+}
+
+int orc_quadrature_points(int dim, const double *coords, int64_t n_cell, const int64_t *cells, int acc,
+                          double *points) {
+  const double *pts;
+  int nq;
+  if ((dim != 2 && dim != 3) || quad_rule(dim, acc, &pts, &nq)) return -1;
+  const int nv = dim + 1;
+  double vx[12], gp[3], Jxw, val[10];
+  for (int64_t e = 0; points && e < n_cell; ++e) {
+    for (int a = 0; a < nv; ++a)
+      for (int d = 0; d < dim; ++d) vx[a * dim + d] = coords[cells[e * nv + a] * dim + d];
+    for (int l = 0; l < nq; ++l) {
+      quad_point(dim, 1, vx, pts + l * nv, gp, &Jxw, val);
+      for (int d = 0; d < dim; ++d) points[(e * nq + l) * dim + d] = gp[d];
+    }
+  }
+  return nq;
+}
+
+/* Operator::L2Discretize (Operator.discretize.templates.h): of a point
+ * function given by its values fq [n_cell*nq] at the quadrature points
+ * (lines 151-183), or of a FEM function u [n_dof] on the same space
+ * (lines 18-47, FEMFunction::value of FEMSpace.templates.h:1087-1100) */
+int orc_l2_discretize(int dim, int degree, const double *coords, int64_t n_cell, const int64_t *cells,
+                      const int32_t *elem_dof, int64_t n_dof, int acc, const double *fq, const double *u,
+                      double *f1) {
+  const double *pts;
+  int nq;
+  if ((dim != 2 && dim != 3) || (degree != 1 && degree != 2) || quad_rule(dim, acc, &pts, &nq)) return -1;
+  if ((fq == NULL) == (u == NULL)) return -1;
+  const int nv = dim + 1, nd = dim == 2 ? 3 * degree : (degree == 1 ? 4 : 10);
+  memset(f1, 0, sizeof(double) * n_dof);
+  double vx[12], gp[3], Jxw, val[10];
+  for (int64_t e = 0; e < n_cell; ++e) {
+    for (int a = 0; a < nv; ++a)
+      for (int d = 0; d < dim; ++d) vx[a * dim + d] = coords[cells[e * nv + a] * dim + d];
+    const int32_t *dof = elem_dof + e * nd;
+    for (int l = 0; l < nq; ++l) {
+      quad_point(dim, degree, vx, pts + l * nv, gp, &Jxw, val);
+      double f = 0;
+      if (fq) f = fq[e * nq + l];
+      else
+        for (int j = 0; j < nd; ++j) f += u[dof[j]] * val[j];
+      for (int j = 0; j < nd; ++j) f1[dof[j]] += Jxw * f * val[j];
+    }
+  }
+  return 0;
+}
+
 void orc_vmult(const orc_csr *a, const double *src, double *dst) {
   for (int64_t i = 0; i < a->m; ++i) {
     dst[i] = 0;

@@ -35,6 +35,15 @@ void orc_csr_free(orc_csr *a);
  * The stiffness element matrix is multiplied by coef[e] when coef != NULL.
  * Both matrices share one pattern: mass_vals receives the mass values in the
  * stiffness pattern's order (pass NULL to skip).  Returns 0 on success. */
+/* quadrature points [n_cell*nq*dim] of the rule of accuracy acc; returns nq
+ * (points may be NULL) or -1 */
+int orc_quadrature_points(int dim, const double *coords, int64_t n_cell, const int64_t *cells, int acc,
+                          double *points);
+/* Operator::L2Discretize of point values fq [n_cell*nq] or of a FEM function
+ * u [n_dof] (exactly one non-NULL) into f1 [n_dof] */
+int orc_l2_discretize(int dim, int degree, const double *coords, int64_t n_cell, const int64_t *cells,
+                      const int32_t *elem_dof, int64_t n_dof, int acc, const double *fq, const double *u,
+                      double *f1);
 int orc_assemble(int dim, int degree, const double *coords, int64_t n_cell,
                  const int64_t *cells, const int32_t *elem_dof, int64_t n_dof,
                  int acc_stiff, int acc_mass, const double *coef,

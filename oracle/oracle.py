@@ -65,6 +65,9 @@ def lib():
         _lib.orc_csr_free.argtypes = [C.POINTER(_CSR)]
         _lib.orc_amg_setup_lazy.argtypes = [C.POINTER(_CSR), C.c_int, C.c_int64, C.c_double, C.POINTER(_AMG)]
         _lib.orc_amg_lazy_reinit.argtypes = [C.POINTER(_AMG), C.POINTER(_CSR)]
+        _lib.orc_quadrature_points.argtypes = [C.c_int, _f64p, C.c_int64, _i64p, C.c_int, _f64p]
+        _lib.orc_l2_discretize.argtypes = [C.c_int, C.c_int, _f64p, C.c_int64, _i64p, _i32p, C.c_int64, C.c_int,
+                                           _f64p, _f64p, _f64p]
     return _lib
 
 
@@ -137,6 +140,37 @@ def assemble(space, acc_stiff, acc_mass, coef=None):
     lib().orc_csr_free(C.byref(out))
     del nnz_guess
     return K, mass
+
+
+def quadrature_points(space, acc):
+    """[n_cell, nq, dim] global quadrature points of the rule of accuracy acc."""
+    mesh = space.mesh
+    coords = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+    cells = np.ascontiguousarray(mesh.cells, dtype=np.int64)
+    nq = lib().orc_quadrature_points(mesh.dim, _ptr(coords, _f64p), mesh.n_cell, _ptr(cells, _i64p), acc, None)
+    if nq < 0:
+        raise RuntimeError("orc_quadrature_points failed")
+    pts = np.empty((mesh.n_cell, nq, mesh.dim))
+    lib().orc_quadrature_points(mesh.dim, _ptr(coords, _f64p), mesh.n_cell, _ptr(cells, _i64p), acc,
+                                _ptr(pts, _f64p))
+    return pts
+
+
+def l2_discretize(space, acc, fq=None, u=None):
+    """Operator::L2Discretize of point values fq [n_cell, nq] or of a FEM function u [n_dof]."""
+    mesh = space.mesh
+    coords = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+    cells = np.ascontiguousarray(mesh.cells, dtype=np.int64)
+    ed = np.ascontiguousarray(space.elem_dof, dtype=np.int32)
+    f1 = np.empty(space.n_dof)
+    fq = None if fq is None else np.ascontiguousarray(fq, dtype=np.float64)
+    u = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+    rc = lib().orc_l2_discretize(mesh.dim, space.degree, _ptr(coords, _f64p), mesh.n_cell, _ptr(cells, _i64p),
+                                 _ptr(ed, _i32p), space.n_dof, acc, None if fq is None else _ptr(fq, _f64p),
+                                 None if u is None else _ptr(u, _f64p), _ptr(f1, _f64p))
+    if rc != 0:
+        raise RuntimeError(f"orc_l2_discretize failed ({rc})")
+    return f1
 
 
 def apply_dirichlet(A: CSR, f, dirichlet, g=None):

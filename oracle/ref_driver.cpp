@@ -42,6 +42,7 @@
 #include <AFEPack/TemplateElement.h>
 #include <AFEPack/FEMSpace.h>
 #include <AFEPack/BilinearOperator.h>
+#include <AFEPack/Operator.h>
 
 using namespace AFEPack;
 
@@ -109,6 +110,9 @@ void dump_csr(const std::string& dir, const std::string& name, const SparseMatri
 }
 
 double zero_fun(const double*) { return 0.0; }
+// source of the L2Discretize fixture: a polynomial, so that any caller that
+// evaluates it at the same points with the same operations gets the same bits
+double poly_fun(const double* p) { return 1.0 + p[0] * p[1] - 2.0 * p[1] * p[1]; }
 
 // Stiffness operator scaled by a per-element coefficient a_e.
 template <int D>
@@ -196,6 +200,17 @@ int run() {
   }
   M.vmult(b, f);
   save_npy(out + "/rhs_mass.npy", &b(0), {n});
+  {
+    // Operator::L2Discretize of a point function and of a FEM function
+    Vector<double> l2;
+    Operator::L2Discretize(&poly_fun, sp, l2, acc_mass);
+    save_npy(out + "/l2_fun.npy", &l2(0), {n});
+    FEMFunction<double, D> fu(sp);
+    for (size_t i = 0; i < n; ++i) fu(i) = f(i);
+    Vector<double> l2u;
+    Operator::L2Discretize(fu, l2u, acc_mass);
+    save_npy(out + "/l2_fem.npy", &l2u(0), {n});
+  }
 
   FEMFunction<double, D> u(sp);
   BoundaryFunction<double, D> bc(BoundaryConditionInfo::DIRICHLET, 1, &zero_fun);

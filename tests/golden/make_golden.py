@@ -67,6 +67,7 @@ def make(name, spec):
                "elem_dof": np.load(os.path.join(d, "elem_dof.npy")),
                "dof_bmark": np.load(os.path.join(d, "dof_bmark.npy")),
                "rhs_mass": np.load(os.path.join(d, "rhs_mass.npy")), "rhs": np.load(os.path.join(d, "rhs.npy")),
+               "l2_fun": np.load(os.path.join(d, "l2_fun.npy")), "l2_fem": np.load(os.path.join(d, "l2_fem.npy")),
                "x_vcycle": np.load(os.path.join(d, "x_vcycle.npy")), "x_pcg": np.load(os.path.join(d, "x_pcg.npy")),
                "n_project": meta["n_project"], "pcg_iters": meta["pcg_iters"]}
         if coef is not None:

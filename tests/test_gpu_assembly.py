@@ -104,3 +104,69 @@ def test_bad_input_is_an_error_not_a_fault(ctx):
     with pytest.raises(N.AFPError) as e:
         Space(ctx, sp)
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("dim,degree,n", [(2, 1, 64), (2, 2, 40), (3, 1, 12), (3, 2, 7)])
+def test_device_dof_numbering_matches_buildDof(ctx, dim, degree, n):
+    """afp_space_create_numbered: the DOF map, boundary marks and points equal
+    the host numbering of FEMSpace::buildDof's order, and so do the matrices."""
+    from afepack_gb300.fem import Space, assemble
+    from afepack_gb300.mesh import FESpace, cube_mesh, square_mesh
+    mesh = square_mesh(n, 0.2, 3) if dim == 2 else cube_mesh(n, 0.15, 3)
+    host = FESpace(mesh, degree)
+    dev = Space.numbered(ctx, mesh, degree)
+    ed, bm, pt = dev.dofs()
+    assert dev.n_dof == host.n_dof
+    assert np.array_equal(ed, host.elem_dof)
+    assert np.array_equal(bm, host.dof_bmark)
+    assert np.array_equal(pt, host.dof_point)
+    acc = {(2, 1): (4, 4), (2, 2): (4, 4), (3, 1): (2, 4), (3, 2): (4, 4)}[(dim, degree)]
+    K1, _ = assemble(dev, *acc)
+    K2, _ = assemble(Space(ctx, host), *acc)
+    for a, b in zip(K1.download(), K2.download()):
+        assert np.array_equal(a, b)
+
+
+def _poly(pts):
+    x, y = pts[..., 0], pts[..., 1]
+    return 1.0 + x * y - 2.0 * y * y
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_l2_discretize_matches_reference(ctx, name):
+    """Operator::L2Discretize on the GPU, bitwise against AFEPack: a point
+    function at the device's quadrature points, and a FEM function."""
+    from afepack_gb300.fem import L2Discretize, Space, quadrature_points
+    g = load_golden(name)
+    host = golden_space(g)
+    sp = Space(ctx, host)
+    acc = int(g["acc_mass"])
+    assert np.array_equal(quadrature_points(sp, acc), O.quadrature_points(host, acc))
+    assert np.array_equal(L2Discretize(_poly, sp, acc), g["l2_fun"])
+    assert np.array_equal(L2Discretize(g["f"], sp, acc), g["l2_fem"])
+
+
+@pytest.mark.parametrize("dim,degree,n", [(2, 2, 96), (3, 1, 40), (3, 2, 8)])
+def test_l2_discretize_matches_oracle(ctx, dim, degree, n):
+    """Larger meshes against the oracle: bitwise for point values and FEM
+    functions (3D P1 40^3 has 384,000 cells, more than one 256 MB chunk of
+    terms, so the per-DOF sums continue across chunks); device-evaluated
+    Gaussians within 1e-14 of the oracle fed numpy's values."""
+    from afepack_gb300.fem import Gaussians, L2Discretize, Space
+    from afepack_gb300.mesh import FESpace, cube_mesh, square_mesh
+    mesh = square_mesh(n, 0.2, 4) if dim == 2 else cube_mesh(n, 0.15, 4)
+    host = FESpace(mesh, degree)
+    sp = Space(ctx, host)
+    acc = 4
+    pts = O.quadrature_points(host, acc)
+    assert np.array_equal(L2Discretize(_poly, sp, acc), O.l2_discretize(host, acc, fq=_poly(pts)))
+    u = np.random.default_rng(7).uniform(-1, 1, host.n_dof)
+    assert np.array_equal(L2Discretize(u, sp, acc), O.l2_discretize(host, acc, u=u))
+    rng = np.random.default_rng(8)
+    c, s = rng.uniform(0.2, 0.8, (8, dim)), rng.uniform(0.05, 0.2, 8)
+    fq = np.zeros(pts.shape[:2])
+    for cc, ss in zip(c, s):
+        fq += np.exp(-np.sum((pts - cc) ** 2, axis=-1) / (2.0 * ss * ss))
+    ref = O.l2_discretize(host, acc, fq=fq)
+    got = L2Discretize(Gaussians(c, s), sp, acc)
+    assert np.max(np.abs(got - ref)) <= 1e-14 * np.max(np.abs(ref))

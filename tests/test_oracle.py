@@ -90,3 +90,21 @@ def test_from_levels_with_given_coarse_inverse():
     x2, it2, _ = given.pcg(b, 1e-10)
     assert it1 == it2
     assert np.abs(x1 - x2).max() <= 1e-10 * np.abs(x1).max()
+
+
+def poly_source(pts):
+    """The fixture's point function, 1 + x y - 2 y^2, in the driver's operation order."""
+    x, y = pts[..., 0], pts[..., 1]
+    return 1.0 + x * y - 2.0 * y * y
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_l2_discretize_matches_reference(name):
+    """Operator::L2Discretize of a point function (evaluated at the oracle's
+    quadrature points) and of a FEM function, bitwise against AFEPack."""
+    g = load_golden(name)
+    sp = golden_space(g)
+    acc = int(g["acc_mass"])
+    fq = poly_source(O.quadrature_points(sp, acc))
+    assert np.array_equal(O.l2_discretize(sp, acc, fq=fq), g["l2_fun"])
+    assert np.array_equal(O.l2_discretize(sp, acc, u=g["f"]), g["l2_fem"])
