@@ -19,6 +19,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <unordered_map>
 
 #include "amg_internal.cuh"
@@ -84,9 +85,11 @@ __global__ void k_dense_gemm(int64_t n, const X* __restrict__ M, const X* __rest
 
 // --------------------------------------------------- V-cycle row kernels
 // One kernel for every row operation of the batched V-cycle on rows [r0, r1)
-// of an n x k block.  A group of W lanes (a power of two, W >= k up to 32)
-// holds the row's k columns, lane l owning columns l, l + W, ... (KPL of
-// them); SPL groups share one row, group p taking the row's entries in chunks
+// of an n x k block.  A group of W lanes (a power of two) holds the row's k
+// columns, KPL per lane: with VEC, lane l owns the contiguous columns
+// l*KPL .. l*KPL+KPL-1 (k == W*KPL) and gathers them with one vector load;
+// otherwise lane l owns columns l, l + W, ... (W >= k up to 32, scalar
+// loads).  SPL groups share one row, group p taking the row's entries in chunks
 // p, p + SPL, ... of W (long coarse-level rows: enough groups in flight to
 // cover the gather latency).  A chunk's (column, value) pairs are loaded one
 // per lane and broadcast with shuffles; the gathers of the x rows of U = 8
@@ -97,7 +100,22 @@ enum RowOp { RO_SPMM = 0, RO_SPMM_ADD, RO_RES, RO_GS, RO_JAC };
 
 constexpr int ROWS_BLK = 256;
 
-template <int W, int KPL, int SPL, class V, class X, int OP>
+// KPL consecutive values at p (16-byte aligned) into v: one vector load
+template <int KPL, class X>
+__device__ __forceinline__ void load_vec(const X* p, X (&v)[KPL]) {
+  if constexpr (std::is_same_v<X, float> && KPL == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  } else if constexpr (std::is_same_v<X, double> && KPL == 2) {
+    const double2 t = *reinterpret_cast<const double2*>(p);
+    v[0] = t.x; v[1] = t.y;
+  } else {
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) v[q] = p[q];
+  }
+}
+
+template <int W, int KPL, int SPL, class V, class X, int OP, bool VEC>
 __global__ void __launch_bounds__(ROWS_BLK) k_rows_m(int64_t r0, int64_t r1, const int* __restrict__ rp,
                                                      const int* __restrict__ ci, const V* __restrict__ va, const X* x,
                                                      X* y, const X* __restrict__ r, const X* __restrict__ d, int k) {
@@ -150,10 +168,17 @@ __global__ void __launch_bounds__(ROWS_BLK) k_rows_m(int64_t r0, int64_t r1, con
             const A val = __shfl_sync(mask, vv, in ? jj + u : 0, W);
             vals[u] = in ? val : A(0);
             const X* xr = x + (int64_t)col * k;
+            if constexpr (VEC) {
+              if (in) load_vec<KPL>(xr + lane * KPL, xv[u]);
+              else
 #pragma unroll
-            for (int q = 0; q < KPL; ++q) {
-              const int c = lane + W * q;
-              xv[u][q] = (in && c < k) ? xr[c] : X(0);
+                for (int q = 0; q < KPL; ++q) xv[u][q] = X(0);
+            } else {
+#pragma unroll
+              for (int q = 0; q < KPL; ++q) {
+                const int c = lane + W * q;
+                xv[u][q] = (in && c < k) ? xr[c] : X(0);
+              }
             }
           }
 #pragma unroll
@@ -179,7 +204,7 @@ __global__ void __launch_bounds__(ROWS_BLK) k_rows_m(int64_t r0, int64_t r1, con
   if (!on) return;
 #pragma unroll
   for (int q = 0; q < KPL; ++q) {
-    const int c = lane + W * q;
+    const int c = VEC ? lane * KPL + q : lane + W * q;
     if (c >= k) continue;
     const int64_t o = row * k + c;
     if (OP == RO_SPMM) y[o] = (X)acc[q];
@@ -190,23 +215,26 @@ __global__ void __launch_bounds__(ROWS_BLK) k_rows_m(int64_t r0, int64_t r1, con
   }
 }
 
-// Launches k_rows_m with W = the smallest power of two >= k (at most 32),
-// KPL = columns per lane, and SPL groups per row for rows of about
-// `row_len` entries (about 48 entries per group).
+// Launches k_rows_m with 16-byte vector gathers (KPL = 16 bytes of columns
+// per lane, W = k / KPL lanes) when k allows them and x is aligned, else
+// with W = the smallest power of two >= k (at most 32) and KPL = columns per
+// lane; SPL groups per row for rows of about `row_len` entries (about 48
+// entries per group).
 template <class V, class X, int OP>
 void rows_m(const afp_context* ctx, int64_t r0, int64_t r1, const int* rp, const int* ci, const V* va, const X* x,
             X* y, const X* r, const X* d, int k, double row_len, const char* what) {
   if (r1 <= r0) return;
   int spl = 1;
   while (spl < 8 && spl * 48 < row_len) spl *= 2;
-  auto go = [&](auto Wc, auto Kc) {
+  auto go = [&](auto Wc, auto Kc, auto Vc) {
     constexpr int W = decltype(Wc)::value, KPL = decltype(Kc)::value;
+    constexpr bool VEC = decltype(Vc)::value;
     auto launch = [&](auto Sc) {
       constexpr int SPL = decltype(Sc)::value;
       constexpr int rows_per_blk = ROWS_BLK / W / SPL > 0 ? ROWS_BLK / W / SPL : 1;
       static_assert(ROWS_BLK / W >= SPL, "a block holds whole rows");
       const unsigned grid = (unsigned)((r1 - r0 + rows_per_blk - 1) / rows_per_blk);
-      k_rows_m<W, KPL, SPL, V, X, OP><<<grid, ROWS_BLK, 0, ctx->stream>>>(r0, r1, rp, ci, va, x, y, r, d, k);
+      k_rows_m<W, KPL, SPL, V, X, OP, VEC><<<grid, ROWS_BLK, 0, ctx->stream>>>(r0, r1, rp, ci, va, x, y, r, d, k);
     };
     if (spl == 1) launch(std::integral_constant<int, 1>());
     else if (spl == 2) launch(std::integral_constant<int, 2>());
@@ -215,13 +243,24 @@ void rows_m(const afp_context* ctx, int64_t r0, int64_t r1, const int* rp, const
   };
   using I1 = std::integral_constant<int, 1>;
   using I2 = std::integral_constant<int, 2>;
-  if (k == 1) go(I1(), I1());
-  else if (k == 2) go(std::integral_constant<int, 2>(), I1());
-  else if (k <= 4) go(std::integral_constant<int, 4>(), I1());
-  else if (k <= 8) go(std::integral_constant<int, 8>(), I1());
-  else if (k <= 16) go(std::integral_constant<int, 16>(), I1());
-  else if (k <= 32) go(std::integral_constant<int, 32>(), I1());
-  else go(std::integral_constant<int, 32>(), I2());
+  using NV = std::false_type;
+  using VV = std::true_type;
+  constexpr int KV = 16 / (int)sizeof(X);  // columns in one 16-byte load
+  const bool vec = k % KV == 0 && k / KV >= 4 && k / KV <= 32 && ((k / KV) & (k / KV - 1)) == 0 &&
+                   reinterpret_cast<uintptr_t>(x) % 16 == 0;
+  if (vec) {
+    constexpr std::integral_constant<int, KV> KVc{};
+    if (k / KV == 4) go(std::integral_constant<int, 4>(), KVc, VV());
+    else if (k / KV == 8) go(std::integral_constant<int, 8>(), KVc, VV());
+    else if (k / KV == 16) go(std::integral_constant<int, 16>(), KVc, VV());
+    else go(std::integral_constant<int, 32>(), KVc, VV());
+  } else if (k == 1) go(I1(), I1(), NV());
+  else if (k == 2) go(std::integral_constant<int, 2>(), I1(), NV());
+  else if (k <= 4) go(std::integral_constant<int, 4>(), I1(), NV());
+  else if (k <= 8) go(std::integral_constant<int, 8>(), I1(), NV());
+  else if (k <= 16) go(std::integral_constant<int, 16>(), I1(), NV());
+  else if (k <= 32) go(std::integral_constant<int, 32>(), I1(), NV());
+  else go(std::integral_constant<int, 32>(), I2(), NV());
   check_launch(ctx, what);
 }
 
