@@ -70,6 +70,8 @@ struct MultiState {
   DevBuf<double> B, Xs, Rs, Z, P, Q, Tmp;   // level-0 CG blocks, n x k
   DevBuf<double> scal;                      // column scalars, 8 x k
   DevBuf<int> active;                       // k flags
+  DevBuf<float2> tail_part;                 // split-inner-dimension partial pairs of the dense tail
+  int tail_split = 1;
   cudaGraphExec_t graph = nullptr;
   int64_t graph_nodes = 0;
   ~MultiState() {

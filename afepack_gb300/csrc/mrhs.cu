@@ -328,6 +328,76 @@ __global__ void __launch_bounds__(256) k_tail_gemm_df(int64_t n, int64_t ld, con
   }
 }
 
+// The same product for wide blocks (k a multiple of 4, at most 64), register
+// tiled: 256 threads = 16 row groups x 16 column groups, each thread a 4 x 4
+// tile of a 64-row x 64-column block tile, so one 16-byte shared load of hi,
+// lo and R each feeds 16 products.  The inner dimension is split into
+// gridDim.y parts of jlen; part s writes its pair sums to part[s] and
+// k_tail_reduce_df adds the parts in s order (the result does not depend on
+// timing).
+constexpr int TG_R = 64, TG_J = 32;
+__global__ void __launch_bounds__(256) k_tail_gemm_df_tiled(int64_t n, int64_t ld, const float* __restrict__ hi,
+                                                             const float* __restrict__ lo,
+                                                             const float* __restrict__ R, int k, int64_t jlen,
+                                                             float2* __restrict__ part) {
+  __shared__ __align__(16) float sH[TG_J][TG_R + 4], sL[TG_J][TG_R + 4];
+  __shared__ __align__(16) float sR[TG_J][MAXK];
+  const int tid = threadIdx.x, cg = tid & 15, rg = tid >> 4;
+  const int64_t row0 = (int64_t)blockIdx.x * TG_R;
+  const int64_t jb = (int64_t)blockIdx.y * jlen;
+  const int64_t je = jb + jlen < n ? jb + jlen : n;
+  float sh[4][4], sl[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) sh[i][c] = sl[i][c] = 0.f;
+  for (int64_t j0 = jb; j0 < je; j0 += TG_J) {
+    const int tj = (int)(je - j0 < TG_J ? je - j0 : TG_J);
+    __syncthreads();
+    for (int t = tid; t < TG_R * TG_J; t += 256) {
+      const int r = t / TG_J, jj = t % TG_J;
+      const bool on = row0 + r < n && jj < tj;
+      sH[jj][r] = on ? hi[(row0 + r) * ld + j0 + jj] : 0.f;
+      sL[jj][r] = on ? lo[(row0 + r) * ld + j0 + jj] : 0.f;
+    }
+    for (int t = tid; t < TG_J * MAXK; t += 256) {
+      const int jj = t / MAXK, c = t % MAXK;
+      sR[jj][c] = (jj < tj && c < k) ? R[(j0 + jj) * k + c] : 0.f;
+    }
+    __syncthreads();
+    for (int jj = 0; jj < tj; ++jj) {
+      const float4 h4 = *reinterpret_cast<const float4*>(&sH[jj][rg * 4]);
+      const float4 l4 = *reinterpret_cast<const float4*>(&sL[jj][rg * 4]);
+      const float4 v4 = *reinterpret_cast<const float4*>(&sR[jj][cg * 4]);
+      const float h[4] = {h4.x, h4.y, h4.z, h4.w}, l[4] = {l4.x, l4.y, l4.z, l4.w};
+      const float v[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) df_add_prod(sh[i][c], sl[i][c], h[i], l[i], v[c]);
+    }
+  }
+  float2* out = part + (int64_t)blockIdx.y * n * k;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int64_t row = row0 + rg * 4 + i;
+    if (row >= n) continue;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int col = cg * 4 + c;
+      if (col < k) out[row * k + col] = make_float2(sh[i][c], sl[i][c]);
+    }
+  }
+}
+
+__global__ void k_tail_reduce_df(int64_t nk, int parts, const float2* __restrict__ part, float* __restrict__ X) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nk) return;
+  float h = part[t].x, l = part[t].y;
+  for (int s = 1; s < parts; ++s) df_add(h, l, part[s * nk + t].x, part[s * nk + t].y);
+  X[t] = __fadd_rn(h, l);
+}
+
 template <class X>
 __global__ void k_diag_solve_m(int64_t n, const int* __restrict__ rp, const X* __restrict__ va,
                                const X* __restrict__ r, X* __restrict__ x, int k) {
@@ -574,6 +644,14 @@ void vcycle_m(afp_amg* h, MultiState& S) {
         k_dense_gemm<KPL, X><<<rows_grid(ctx, T.n), BLK, 0, ctx->stream>>>(T.n, h->tail_inv.get(), blk<X>(S, 1, t),
                                                                           blk<X>(S, 0, t), k);
       });
+    } else if (S.tail_split > 0 && S.tail_part.size() > 0) {
+      const int64_t rb = (T.n + TG_R - 1) / TG_R;
+      const int64_t jlen = ((T.n + S.tail_split - 1) / S.tail_split + TG_J - 1) / TG_J * TG_J;
+      const int parts = (int)((T.n + jlen - 1) / jlen);
+      k_tail_gemm_df_tiled<<<dim3((unsigned)rb, (unsigned)parts), 256, 0, ctx->stream>>>(
+          T.n, h->tail_ld, h->tail_hi.get(), h->tail_lo.get(), blk<X>(S, 1, t), k, jlen, S.tail_part.get());
+      k_tail_reduce_df<<<grid_for(T.n * k, BLK), BLK, 0, ctx->stream>>>(T.n * k, parts, S.tail_part.get(),
+                                                                        blk<X>(S, 0, t));
     } else {
       constexpr int TR = 16;
       k_tail_gemm_df<TR><<<(unsigned)((T.n + TR - 1) / TR), 256, 0, ctx->stream>>>(
@@ -634,6 +712,16 @@ void ensure_state(afp_amg* h, int k) {
   S->scal.alloc(ctx, 8 * MAXK + (int64_t)RED_GRID * MAXK + 1);  // scalars, partials, retire counter
   S->scal.zero();
   S->active.alloc(ctx, MAXK);
+  // the register-tiled tail product for wide FP32 blocks: split its inner
+  // dimension so that the grid covers about four waves of the GPU
+  const Level& T = h->lv[h->t];
+  if (mixed && h->tail_dense && k >= 32 && k % 4 == 0) {
+    const int64_t rb = (T.n + TG_R - 1) / TG_R;
+    S->tail_split = (int)std::max<int64_t>(1, std::min<int64_t>(8, (4 * ctx->sm_count + rb - 1) / rb));
+    S->tail_part.alloc(ctx, (int64_t)S->tail_split * T.n * k);
+  } else {
+    S->tail_split = 0;
+  }
   h->multi = std::move(S);
 }
 
