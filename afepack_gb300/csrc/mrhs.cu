@@ -961,6 +961,28 @@ namespace {
 using SClock = std::chrono::steady_clock;
 double s_secs(SClock::time_point a, SClock::time_point b) { return std::chrono::duration<double>(b - a).count(); }
 
+// Pinned host staging of the driver: k columns in, k columns out, and the
+// column scalars read after every iteration.
+struct PinnedStage {
+  double* in = nullptr;
+  double* out = nullptr;
+  double* scal = nullptr;
+  PinnedStage(int64_t n, int k) {
+    AFP_CUDA(cudaMallocHost(&in, sizeof(double) * n * k));
+    AFP_CUDA(cudaMallocHost(&out, sizeof(double) * n * k));
+    AFP_CUDA(cudaMallocHost(&scal, sizeof(double) * 5 * afp::MAXK));
+  }
+  ~PinnedStage() {
+    cudaFreeHost(in);
+    cudaFreeHost(out);
+    cudaFreeHost(scal);
+  }
+};
+
+// The driver keeps the GPU busy between CG iterations: admissions copy the
+// right-hand side through pinned memory (one asynchronous copy each), and a
+// retired column's solution is copied out asynchronously and handed to its
+// waiter while the next iteration runs.
 void batch_driver(afp_batch_server* s) {
   using namespace afp;
   afp_amg* h = s->amg;
@@ -968,13 +990,39 @@ void batch_driver(afp_batch_server* s) {
   const int k = s->opts.width;
   std::vector<afp_batch_server::Req*> slot(k, nullptr);
   std::vector<int> iters(k, 0), act(k, 0);
-  std::vector<double> host(5 * MAXK);
+  std::vector<double> rz_one(afp::MAXK, 1.0);
+  // retired columns whose solutions are on their way to pinned memory
+  std::vector<std::pair<int, afp_batch_server::Req*>> leaving;
+  cudaEvent_t out_done = nullptr;
+  auto hand_over = [&](double* pin_out, int64_t n) {
+    if (leaving.empty()) return;
+    AFP_CUDA(cudaEventSynchronize(out_done));
+    for (auto& [c, r] : leaving) r->x.assign(pin_out + (int64_t)c * n, pin_out + (int64_t)(c + 1) * n);
+    const auto now = SClock::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (auto& [c, r] : leaving) {
+      r->res.queue_seconds = s_secs(r->t_submit, r->t_admit);
+      r->res.latency_seconds = s_secs(r->t_submit, now);
+      r->done = true;
+      if (r->res.status == AFP_OK) {
+        s->completed++;
+        s->latencies.push_back(r->res.latency_seconds);
+      } else {
+        s->failed++;
+      }
+      s->t_last = now;
+    }
+    leaving.clear();
+    s->cv_done.notify_all();
+  };
   try {
     bind(ctx);
     ensure_state(h, k);
     MultiState& S = *h->multi;
     const Level& L0 = h->lv[0];
     const int64_t n = L0.n;
+    PinnedStage pin(n, k);
+    AFP_CUDA(cudaEventCreateWithFlags(&out_done, cudaEventDisableTiming));
     double* sc = S.scal.get();  // rows: 0 rz (old), 1 pq, 2 rr, 3 rz (new), 4 bb
     double* partials = sc + 8 * MAXK;
     const CSRView<double> A = L0.A<double>();
@@ -990,6 +1038,11 @@ void batch_driver(afp_batch_server* s) {
       {
         std::unique_lock<std::mutex> lk(s->mu);
         const bool any_active = std::find(act.begin(), act.end(), 1) != act.end();
+        if (!any_active && !leaving.empty()) {
+          lk.unlock();
+          hand_over(pin.out, n);
+          lk.lock();
+        }
         if (!any_active) s->cv_work.wait(lk, [&] { return s->stop || !s->queue.empty(); });
         if (s->stop && s->queue.empty() && !any_active) break;
         for (int c = 0; c < k && !s->queue.empty(); ++c)
@@ -1002,16 +1055,20 @@ void batch_driver(afp_batch_server* s) {
       }
       if (!admit.empty()) {
         for (auto& [c, r] : admit) {
-          copy(ctx, S.Tmp.get() + (int64_t)c * n, r->b.data(), sizeof(double) * n);
+          double* stage = pin.in + (int64_t)c * n;
+          std::memcpy(stage, r->b.data(), sizeof(double) * n);
+          std::vector<double>().swap(r->b);
+          AFP_CUDA(cudaMemcpyAsync(S.Tmp.get() + (int64_t)c * n, stage, sizeof(double) * n, cudaMemcpyHostToDevice,
+                                   ctx->stream));
           k_col_admit<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, k, c, L0.perm.get(), S.Tmp.get() + (int64_t)c * n,
                                                                 S.B.get(), S.Xs.get(), S.Rs.get(), S.P.get());
           check_launch(ctx, "batch admit");
+          // old r.z of a fresh column: 1
+          AFP_CUDA(cudaMemcpyAsync(sc + c, rz_one.data(), sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
           slot[c] = r;
           iters[c] = 0;
           act[c] = 1;
-          host[c] = 1.0;  // old r.z of a fresh column
         }
-        for (auto& [c, r] : admit) copy(ctx, sc + c, &host[c], sizeof(double));
         S.active.upload(act.data(), k);
         with_kpl(k, [&](auto KPLc) {
           constexpr int KPL = decltype(KPLc)::value;
@@ -1036,57 +1093,48 @@ void batch_driver(afp_batch_server* s) {
         check_launch(ctx, "batch x r");
       });
       AFP_CUDA(cudaMemcpyAsync(sc, sc + 3 * MAXK, sizeof(double) * k, cudaMemcpyDeviceToDevice, ctx->stream));
-      copy(ctx, host.data() + 2 * MAXK, sc + 2 * MAXK, sizeof(double) * 3 * MAXK);  // rr, rz, bb
+      AFP_CUDA(cudaMemcpyAsync(pin.scal + 2 * MAXK, sc + 2 * MAXK, sizeof(double) * 3 * MAXK,
+                               cudaMemcpyDeviceToHost, ctx->stream));  // rr, rz, bb
+      // the previous retirements' solutions arrived before this iteration started
+      hand_over(pin.out, n);
       sync(ctx);
       // ---- retire converged (or failed) columns
-      std::vector<std::pair<int, int>> out;  // (column, status)
+      const double* host = pin.scal;
+      bool retired = false;
       for (int c = 0; c < k; ++c) {
         if (!act[c]) continue;
         ++iters[c];
         const double bn = std::max(std::sqrt(host[4 * MAXK + c]), 1e-300);
         const double rel = std::sqrt(host[2 * MAXK + c]) / bn;
-        slot[c]->res.rel_residual = rel;
-        if (!std::isfinite(rel)) out.push_back({c, AFP_ERR_BREAKDOWN});
-        else if (rel <= s->opts.tol) out.push_back({c, AFP_OK});
-        else if (iters[c] >= s->opts.maxit) out.push_back({c, AFP_ERR_NOT_CONVERGED});
-      }
-      for (auto& [c, st] : out) {
         afp_batch_server::Req* r = slot[c];
+        r->res.rel_residual = rel;
+        int st = -1;
+        if (!std::isfinite(rel)) st = AFP_ERR_BREAKDOWN;
+        else if (rel <= s->opts.tol) st = AFP_OK;
+        else if (iters[c] >= s->opts.maxit) st = AFP_ERR_NOT_CONVERGED;
+        if (st < 0) continue;
         k_col_retire<<<grid_for(n, BLK), BLK, 0, ctx->stream>>>(n, k, c, L0.perm.get(), S.Xs.get(),
                                                                S.Tmp.get() + (int64_t)c * n, S.Rs.get(), S.P.get());
         check_launch(ctx, "batch retire");
-        r->x.resize(n);
-        copy(ctx, r->x.data(), S.Tmp.get() + (int64_t)c * n, sizeof(double) * n);
+        AFP_CUDA(cudaMemcpyAsync(pin.out + (int64_t)c * n, S.Tmp.get() + (int64_t)c * n, sizeof(double) * n,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
         r->res.status = st;
         r->res.iterations = iters[c];
+        leaving.push_back({c, r});
+        slot[c] = nullptr;
         act[c] = 0;
+        retired = true;
       }
-      if (!out.empty()) {
+      if (retired) {
+        AFP_CUDA(cudaEventRecord(out_done, ctx->stream));
         S.active.upload(act.data(), k);
-        sync(ctx);
-        const auto now = SClock::now();
-        std::lock_guard<std::mutex> lk(s->mu);
-        for (auto& [c, st] : out) {
-          afp_batch_server::Req* r = slot[c];
-          slot[c] = nullptr;
-          r->res.queue_seconds = s_secs(r->t_submit, r->t_admit);
-          r->res.latency_seconds = s_secs(r->t_submit, now);
-          r->done = true;
-          if (st == AFP_OK) {
-            s->completed++;
-            s->latencies.push_back(r->res.latency_seconds);
-          } else {
-            s->failed++;
-          }
-          s->t_last = now;
-        }
-        s->cv_done.notify_all();
       }
       {
         std::lock_guard<std::mutex> lk(s->mu);
         s->iterations++;
       }
     }
+    hand_over(pin.out, n);
   } catch (const Error& e) {
     std::lock_guard<std::mutex> lk(s->mu);
     s->fatal = e.msg;
@@ -1099,6 +1147,7 @@ void batch_driver(afp_batch_server* s) {
     s->queue.clear();
     s->cv_done.notify_all();
   }
+  if (out_done) cudaEventDestroy(out_done);
 }
 
 double s_percentile(std::vector<double> v, double p) {

@@ -93,6 +93,33 @@ def test_one_poisoned_request_fails_alone_in_the_server(ctx):
         assert np.array_equal(x, xm)
 
 
+def test_one_poisoned_column_fails_alone_in_the_batch_server(ctx):
+    """Continuous batching against one hierarchy: a NaN right-hand side
+    retires with a breakdown status after its first iteration; the columns
+    beside it finish with bitwise the solutions they get alone, and the
+    server keeps serving."""
+    from afepack_gb300.amg import MIXED
+    from afepack_gb300.serve import BatchServer
+    _, b, amg = _poisson(ctx, 48, MIXED)
+    rng = np.random.default_rng(3)
+    good = [b * (1.0 + 0.2 * rng.standard_normal()) for _ in range(5)]
+    bad = b.copy()
+    bad[7] = np.nan
+    with BatchServer(amg, width=4) as alone:
+        solo = [alone.wait(alone.submit(v)) for v in good]
+    with BatchServer(amg, width=4) as srv:
+        tickets = [srv.submit(v) for v in (good[0], good[1], bad, good[2], good[3], good[4])]
+        out = [srv.wait(t) for t in tickets]
+        after = srv.wait(srv.submit(good[0]))
+        st = srv.stats()
+    assert out[2][1]["status"] == BREAKDOWN and out[2][1]["iterations"] == 1
+    assert st["failed"] == 1 and st["completed"] == 6
+    for (x, r), (xm, rm) in zip(solo, [out[0], out[1], out[3], out[4], out[5]]):
+        assert r["status"] == 0 and rm["status"] == 0
+        assert np.array_equal(x, xm)
+    assert np.array_equal(after[0], solo[0][0])
+
+
 def test_stalled_grid_barrier_times_out_and_the_context_stays_usable(native, ctx):
     """Fault injection on the GPU without a fault: the persistent V-cycle's
     first grid barrier waits for one arrival more than the grid has (a count
