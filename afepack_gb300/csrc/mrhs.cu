@@ -224,22 +224,29 @@ template <class V, class X, int OP>
 void rows_m(const afp_context* ctx, int64_t r0, int64_t r1, const int* rp, const int* ci, const V* va, const X* x,
             X* y, const X* r, const X* d, int k, double row_len, const char* what) {
   if (r1 <= r0) return;
-  int spl = 1;
-  while (spl < 8 && spl * 48 < row_len) spl *= 2;
   auto go = [&](auto Wc, auto Kc, auto Vc) {
     constexpr int W = decltype(Wc)::value, KPL = decltype(Kc)::value;
     constexpr bool VEC = decltype(Vc)::value;
+    // groups per row: enough for the row's gathers to overlap (about 48
+    // entries per group), and for short row ranges (small colour classes of
+    // coarse levels) enough lanes to fill about half the GPU
+    int spl = 1;
+    while (spl < 8 && spl * 48 < row_len) spl *= 2;
+    while (spl < 16 && spl * W < row_len && (double)(r1 - r0) * W * spl < 1024.0 * ctx->sm_count) spl *= 2;
+    spl = std::min(spl, ROWS_BLK / W);
     auto launch = [&](auto Sc) {
       constexpr int SPL = decltype(Sc)::value;
-      constexpr int rows_per_blk = ROWS_BLK / W / SPL > 0 ? ROWS_BLK / W / SPL : 1;
-      static_assert(ROWS_BLK / W >= SPL, "a block holds whole rows");
-      const unsigned grid = (unsigned)((r1 - r0 + rows_per_blk - 1) / rows_per_blk);
-      k_rows_m<W, KPL, SPL, V, X, OP, VEC><<<grid, ROWS_BLK, 0, ctx->stream>>>(r0, r1, rp, ci, va, x, y, r, d, k);
+      if constexpr (ROWS_BLK / W >= SPL) {  // a block holds whole rows
+        constexpr int rows_per_blk = ROWS_BLK / W / SPL;
+        const unsigned grid = (unsigned)((r1 - r0 + rows_per_blk - 1) / rows_per_blk);
+        k_rows_m<W, KPL, SPL, V, X, OP, VEC><<<grid, ROWS_BLK, 0, ctx->stream>>>(r0, r1, rp, ci, va, x, y, r, d, k);
+      }
     };
     if (spl == 1) launch(std::integral_constant<int, 1>());
     else if (spl == 2) launch(std::integral_constant<int, 2>());
     else if (spl == 4) launch(std::integral_constant<int, 4>());
-    else launch(std::integral_constant<int, 8>());
+    else if (spl == 8) launch(std::integral_constant<int, 8>());
+    else launch(std::integral_constant<int, 16>());
   };
   using I1 = std::integral_constant<int, 1>;
   using I2 = std::integral_constant<int, 2>;
@@ -499,13 +506,37 @@ __global__ void k_spmm_dot(int64_t m, const int* __restrict__ rp, const int* __r
     double acc[KPL];
 #pragma unroll
     for (int q = 0; q < KPL; ++q) acc[q] = 0;
-    for (int j = rp[row]; j < rp[row + 1]; ++j) {
-      const double a = va[j];
-      const double* pr = p + (int64_t)ci[j] * k;
+    // a chunk of 32 (column, value) pairs, one per lane, broadcast with
+    // shuffles; the gathers of U entries are issued before their products
+    // are summed (entries still added in row order)
+    const int e = rp[row + 1];
+    for (int base = rp[row]; base < e; base += 32) {
+      const int my = base + lane;
+      const int cc = my < e ? ci[my] : 0;
+      const double vv = my < e ? va[my] : 0.0;
+      const int cnt = min(32, e - base);
+      constexpr int U = 8;
+      for (int jj = 0; jj < cnt; jj += U) {
+        double vals[U], pv[U][KPL];
 #pragma unroll
-      for (int q = 0; q < KPL; ++q) {
-        const int c = lane + 32 * q;
-        if (c < k) acc[q] += a * pr[c];
+        for (int u = 0; u < U; ++u) {
+          const bool in = jj + u < cnt;  // the same for the whole warp
+          const int col = __shfl_sync(0xffffffffu, cc, in ? jj + u : 0);
+          vals[u] = __shfl_sync(0xffffffffu, vv, in ? jj + u : 0);
+          const double* pr = p + (int64_t)col * k;
+#pragma unroll
+          for (int q = 0; q < KPL; ++q) {
+            const int c = lane + 32 * q;
+            pv[u][q] = (in && c < k) ? pr[c] : 0.0;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (jj + u >= cnt) break;
+#pragma unroll
+          for (int q = 0; q < KPL; ++q)
+            if (lane + 32 * q < k) acc[q] += vals[u] * pv[u][q];
+        }
       }
     }
 #pragma unroll
