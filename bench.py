@@ -560,7 +560,10 @@ def run_stream(args):
                 "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 1),
                 "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 1),
                 "failed": int(sum(r["status"] != 0 for r in res)),
-                "iterations_median": int(np.median([r["iterations"] for r in res]))}
+                "iterations_median": int(np.median([r["iterations"] for r in res])),
+                # where a request's time goes: admission -> hierarchy ready, and the CG on the device
+                "setup_s_total": round(float(sum(r["setup_seconds"] for r in res)), 2),
+                "cg_device_s_total": round(float(sum(r["device_seconds"] for r in res)), 2)}
 
     out = {}
     for name, prec in (("mixed", 1), ("fp64", 0)):
