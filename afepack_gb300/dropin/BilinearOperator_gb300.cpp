@@ -6,8 +6,10 @@
 //
 // BilinearOperator<D, double, double, D, D, D>::build() (include/AFEPack/
 // BilinearOperator.templates.h:56-60) is specialised for D = 2, 3.  When the
-// object's exact dynamic type is StiffMatrix<D, double> or MassMatrix<D,
-// double> -- not a user subclass that overrides getElementMatrix -- and every
+// object's exact dynamic type is StiffMatrix<D, double>, MassMatrix<D,
+// double> or VarCoeffStiffMatrix<D> (one coefficient per element,
+// VarCoeffStiffMatrix.h) -- not a user subclass that overrides
+// getElementMatrix -- and every
 // element's template takes its basis functions from AFEPack's Lagrange P1/P2
 // triangle or tetrahedron plugin (libtriangle.{1,2}.bas_fun.so,
 // libtetrahedron.{1,2}.bas_fun.so, read from the template's own basis
@@ -33,6 +35,7 @@
 #include <typeinfo>
 #include <vector>
 
+#include "VarCoeffStiffMatrix.h"
 #include "afepack_gb300.h"
 
 AFEPACK_OPEN_NAMESPACE
@@ -103,7 +106,8 @@ int space_degree(const Space& sp) {
 // P1/P2 simplex space; returns false (nothing done) otherwise.
 template <int D>
 bool gpu_build(BilinearOperator<D, double, double, D, D, D>& op) {
-  const bool stiff = typeid(op) == typeid(StiffMatrix<D, double, D, D>);
+  const bool varcoef = typeid(op) == typeid(VarCoeffStiffMatrix<D>);
+  const bool stiff = varcoef || typeid(op) == typeid(StiffMatrix<D, double, D, D>);
   const bool mass = typeid(op) == typeid(MassMatrix<D, double, D, D>);
   if (!stiff && !mass) return false;
   FEMSpace<double, D, D, D>* sp = op.FEMSpace0();
@@ -135,7 +139,17 @@ bool gpu_build(BilinearOperator<D, double, double, D, D, D>& op) {
   afp_space* space = nullptr;
   check(afp_space_create(context(), D, degree, nv, coords.data(), ne, cells.data(), n, elem_dof.data(), &space),
         "afp_space_create");
-  afp_assemble_opts opts{op.algebricAccuracy(), op.algebricAccuracy(), nullptr};
+  const double* coef = nullptr;
+  if (varcoef) {
+    const std::vector<double>& c = static_cast<VarCoeffStiffMatrix<D>&>(op).coefficient();
+    if ((int64_t)c.size() != ne) {
+      std::cerr << "afepack_gb300: VarCoeffStiffMatrix has " << c.size() << " coefficients for " << ne
+                << " elements" << std::endl;
+      abort();
+    }
+    coef = c.data();
+  }
+  afp_assemble_opts opts{op.algebricAccuracy(), op.algebricAccuracy(), coef};
   afp_matrix *K = nullptr, *M = nullptr;
   check(afp_assemble(space, &opts, &K, mass ? &M : nullptr), "afp_assemble");
   afp_matrix* A = stiff ? K : M;

@@ -19,6 +19,7 @@ OBJ = os.path.join(ROOT, "oracle", "_ref", "obj")
 MAIN = r"""
 #include <AFEPack/AMGSolver.h>
 #include <AFEPack/BilinearOperator.h>
+#include "VarCoeffStiffMatrix.h"
 using namespace AFEPack;
 int main(int argc, char**) {
   SparsityPattern sp(1, 1, (size_t)1);
@@ -37,6 +38,9 @@ int main(int argc, char**) {
     FEMSpace<double, 3> fs3;
     StiffMatrix<3, double> K3(fs3);
     K3.build();
+    std::vector<double> coef(1, 2.0);
+    VarCoeffStiffMatrix<2> C2(fs2, coef);
+    C2.build();
   }
   return 0;
 }
@@ -49,7 +53,7 @@ def test_dropin_links_into_afepack(native, tmp_path):
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "-j8", f"REF={REF}"],
                               stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     flags = ["-std=c++20", "-O1", "-w", "-I" + os.path.join(ROOT, "oracle", "shim"), "-I" + os.path.join(REF, "include"),
-             "-I" + os.path.join(ROOT, "include")]
+             "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "afepack_gb300", "dropin")]
     drops = []
     for src in ("AMGSolver_gb300.cpp", "BilinearOperator_gb300.cpp", "dropin_core.cpp"):
         obj = tmp_path / src.replace(".cpp", ".o")
