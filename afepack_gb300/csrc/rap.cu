@@ -79,6 +79,13 @@ __device__ int collect_row(int64_t i, const int* __restrict__ prp, const int* __
       const int b = ac[k];
       for (int l = trp[b]; l < trp[b + 1]; ++l) mine += hash_insert(table, cap, tc[l]);
     }
+    if (GROUP == 32) {
+      // a row that outgrows the warp's table goes to the block pass: stop
+      // here instead of probing a full table for the rest of its products
+      int c = mine;
+      for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+      if (c > limit) return c;
+    }
   }
   // reduce the count
   int cnt = mine;
@@ -92,7 +99,6 @@ __device__ int collect_row(int64_t i, const int* __restrict__ prp, const int* __
     cnt = *red;
     __syncthreads();
   }
-  (void)limit;
   return cnt;
 }
 
@@ -200,7 +206,11 @@ __device__ __forceinline__ int find_slot(const int* c, int R, int key, int row) 
 // memory (their column list too, for the slot searches); longer rows in
 // place in global memory.  acc_cap is sized by the host from the product's
 // longest row, so the nearly dense coarse levels of 3D hierarchies stay in
-// shared memory as well.
+// shared memory as well.  With MAP (coarse levels of at most a few ten
+// thousand rows), each warp also keeps a column -> slot table of n_c
+// entries, so a product finds its entry with one shared load instead of a
+// binary search over the row.
+template <bool MAP>
 __global__ void k_rap_numeric(int64_t n_c, const int* __restrict__ prp, const int* __restrict__ pc,
                               const double* __restrict__ pv, const int* __restrict__ arp, const int* __restrict__ ac,
                               const double* __restrict__ av, const int* __restrict__ trp, const int* __restrict__ tc,
@@ -210,6 +220,13 @@ __global__ void k_rap_numeric(int64_t n_c, const int* __restrict__ prp, const in
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   double* sacc = reinterpret_cast<double*>(sm_num) + (size_t)warp * acc_cap;
   int* scol = reinterpret_cast<int*>(reinterpret_cast<double*>(sm_num) + (size_t)wpb * acc_cap) + warp * acc_cap;
+  unsigned short* smap = reinterpret_cast<unsigned short*>(reinterpret_cast<int*>(
+                             reinterpret_cast<double*>(sm_num) + (size_t)wpb * acc_cap) + (size_t)wpb * acc_cap) +
+                         (size_t)warp * (MAP ? n_c : 0);
+  if (MAP) {
+    for (int64_t t = lane; t < n_c; t += 32) smap[t] = 0xFFFFu;
+    __syncwarp();
+  }
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < n_c; i += (int64_t)gridDim.x * wpb) {
     const int r0 = rowptr[i], R = rowptr[i + 1] - r0;
     const bool in_smem = R <= acc_cap;
@@ -218,6 +235,7 @@ __global__ void k_rap_numeric(int64_t n_c, const int* __restrict__ prp, const in
     for (int t = lane; t < R; t += 32) {
       acc[t] = 0.0;
       if (in_smem) scol[t] = cols[r0 + t];
+      if (MAP) smap[cols[r0 + t]] = (unsigned short)t;
     }
     __syncwarp();
     for (int j = prp[i]; j < prp[i + 1]; ++j) {
@@ -227,7 +245,7 @@ __global__ void k_rap_numeric(int64_t n_c, const int* __restrict__ prp, const in
         const int b = ac[k];
         const double pm = p * av[k];
         for (int l = trp[b] + lane; l < trp[b + 1]; l += 32) {
-          const int slot = find_slot(rc, R, tc[l], (int)i);
+          const int slot = MAP ? (int)smap[tc[l]] : find_slot(rc, R, tc[l], (int)i);
           acc[slot] += pm * tv[l];
         }
         __syncwarp();
@@ -235,6 +253,8 @@ __global__ void k_rap_numeric(int64_t n_c, const int* __restrict__ prp, const in
     }
     if (in_smem)
       for (int t = lane; t < R; t += 32) vals[r0 + t] = sacc[t];
+    if (MAP)
+      for (int t = lane; t < R; t += 32) smap[cols[r0 + t]] = 0xFFFFu;
     __syncwarp();
   }
 }
@@ -302,14 +322,27 @@ void galerkin_product(const afp_context* ctx, int64_t n_c, int64_t n_f, const in
   }
   const size_t per_entry = sizeof(double) + sizeof(int);
   int acc_cap = std::max(1024, (rmax + 31) / 32 * 32);
+  // the column -> slot table: rows long enough for the binary search to
+  // matter (a hundred entries and more) on levels small enough for a table
+  // of n_c 16-bit slots per warp
+  const size_t map_bytes = (size_t)n_c * sizeof(unsigned short);
+  const bool map = rmax >= 128 && rmax < 65535 && map_bytes <= 64 * 1024;
+  const size_t per_warp_extra = map ? (map_bytes + 15) / 16 * 16 : 0;
   int wpn = 4;
-  while (wpn > 1 && (size_t)wpn * acc_cap * per_entry > NUM_SMEM_MAX) --wpn;
-  if ((size_t)acc_cap * per_entry > NUM_SMEM_MAX) acc_cap = (int)(NUM_SMEM_MAX / per_entry) / 32 * 32;  // global
-  const size_t smem_n = (size_t)wpn * acc_cap * per_entry;
+  while (wpn > 1 && (size_t)wpn * (acc_cap * per_entry + per_warp_extra) > NUM_SMEM_MAX) --wpn;
+  if ((size_t)acc_cap * per_entry + per_warp_extra > NUM_SMEM_MAX)  // longest rows accumulate in global memory
+    acc_cap = (int)((NUM_SMEM_MAX - per_warp_extra) / per_entry) / 32 * 32;
+  const size_t smem_n = (size_t)wpn * (acc_cap * per_entry + per_warp_extra);
   const unsigned grid_n = (unsigned)std::min<int64_t>((n_c + wpn - 1) / wpn, (int64_t)ctx->sm_count * 16);
-  AFP_CUDA(cudaFuncSetAttribute(k_rap_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_n));
-  k_rap_numeric<<<grid_n, wpn * 32, smem_n, ctx->stream>>>(n_c, prp, pc, pv, arp, ac, av, trp, tc, tv,
-                                                           out.rowptr.get(), out.cols.get(), vals.get(), acc_cap);
+  if (map) {
+    AFP_CUDA(cudaFuncSetAttribute(k_rap_numeric<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_n));
+    k_rap_numeric<true><<<grid_n, wpn * 32, smem_n, ctx->stream>>>(
+        n_c, prp, pc, pv, arp, ac, av, trp, tc, tv, out.rowptr.get(), out.cols.get(), vals.get(), acc_cap);
+  } else {
+    AFP_CUDA(cudaFuncSetAttribute(k_rap_numeric<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_n));
+    k_rap_numeric<false><<<grid_n, wpn * 32, smem_n, ctx->stream>>>(
+        n_c, prp, pc, pv, arp, ac, av, trp, tc, tv, out.rowptr.get(), out.cols.get(), vals.get(), acc_cap);
+  }
   check_launch(ctx, "rap numeric");
 }
 

@@ -60,6 +60,26 @@ def test_hierarchy_matches_oracle_poisson2d(ctx):
         assert np.array_equal(arp, A.rowptr) and np.array_equal(aci, A.cols) and np.array_equal(ava, A.vals)
 
 
+def test_hierarchy_matches_oracle_poisson3d(ctx):
+    """Every level of the full-depth 3D P1 20^3 hierarchy bitwise against the
+    oracle's: its coarse levels have rows of hundreds of entries, where the
+    Galerkin product's numeric pass finds slots through its column table."""
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.amg import AMGSolver
+    _, K, b = system(ctx, W.poisson3d_p1(20))
+    amg = AMGSolver(K, dense_tail=0)
+    rp, ci, va = K.download()
+    ho = O.AMG(O.CSR(rp, ci, va, (rp.shape[0] - 1,) * 2))
+    assert amg.n_project() == ho.n_level
+    longest = 0
+    for l in range(ho.n_level):
+        A = ho.level(l + 1)
+        arp, aci, ava = amg.level_matrix(l + 1)
+        longest = max(longest, int(np.diff(arp).max()))
+        assert np.array_equal(arp, A.rowptr) and np.array_equal(aci, A.cols) and np.array_equal(ava, A.vals), l
+    assert longest >= 128  # rows long enough for the column table
+
+
 @pytest.mark.parametrize("case", ["poisson2d_p1_256", "poisson3d_p1_24", "elliptic2d_p2_64", "poisson3d_p2_8"])
 def test_gpu_coarsening_matches_host(ctx, case):
     """The GPU C/F splitting and P (gpu_coarsen=1) against the host routine
