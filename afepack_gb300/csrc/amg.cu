@@ -793,7 +793,7 @@ void afp_amg_default_opts(afp_amg_opts* o) {
   o->min_density = 0.382;
   o->alpha = 0.25;
   o->precision = AFP_PRECISION_FP64;
-  o->dense_tail = 2048;
+  o->dense_tail = 4096;
   o->max_colors = 32;
   o->symmetric = 1;
   o->coarse_colors = 4;

@@ -572,7 +572,8 @@ def run_stream(args):
 
     out = {}
     for name, prec in (("mixed", 1), ("fp64", 0)):
-        with Server(workers=args.workers, precision=prec, tol=args.tol) as srv:
+        # independent small requests: a dense tail of at most 2048 rows keeps each setup cheap
+        with Server(workers=args.workers, precision=prec, tol=args.tol, dense_tail=2048) as srv:
             for t in [srv.submit(wl) for wl in wls[: min(4, len(wls))]]:
                 srv.wait(t)
             sat = run(srv, np.zeros(len(wls)))
@@ -589,7 +590,7 @@ def run_stream(args):
         "vs_baseline": None, "dtype": "fp32 V-cycle + fp64 CG", "data": "synthetic (seeded)",
         "config": {"workload": "request_stream", "requests": len(wls), "sample": "every 10th of the 2000-request stream",
                    "workers": args.workers, "n_dof_min": min(ndofs), "n_dof_max": max(ndofs),
-                   "n_dof_total": sum(ndofs), "tol": args.tol, "generation_s": round(gen_s, 2),
+                   "n_dof_total": sum(ndofs), "tol": args.tol, "generation_s": round(gen_s, 2), "dense_tail": 2048,
                    "arrival": "saturation (all at once), then Poisson at 50% of the saturated rate"},
         "p50_ms": m["poisson_50pct"]["p50_ms"], "p99_ms": m["poisson_50pct"]["p99_ms"],
         "mixed": m, "fp64": out["fp64"],

@@ -189,16 +189,17 @@ typedef struct afp_amg_opts {
   double alpha;         /* strong-connection threshold (default 0.25)           */
   int precision;        /* afp_precision of the V-cycle (default FP64)          */
   int dense_tail;       /* coarsening stops at the first coarse level with at
-                           most this many rows (default 2048, max 16384), or
+                           most this many rows (default 4096, max 16384), or
                            with at most 16384 rows and at least 5% of its
                            entries nonzero; that level is solved with a dense
                            inverse instead of smoothed (0 keeps the
                            reference's full depth).  The inverse costs 2 n^3
-                           FP64 operations, so a sparse level of several
-                           thousand rows (a 33K-DOF 2D problem's 7,644-row
-                           third level: 1 s) is coarsened further instead;
-                           dense coarse levels of 3D and 2D P2 hierarchies
-                           (6,744 rows at 12%, 12,588 at 11%) stop by density */
+                           FP64 operations (0.1 s at 4096 rows), so a sparse
+                           level of more rows (a 33K-DOF 2D problem's
+                           7,644-row third level: 1 s) is coarsened further
+                           instead; dense coarse levels of 3D and 2D P2
+                           hierarchies (6,744 rows at 12%, 12,588 at 11%)
+                           stop by density */
   int max_colors;       /* colour classes of the smoother before rows fall into
                            an l1-Jacobi overflow class (default 32)             */
   int symmetric;        /* post-smoothing visits colours in reverse order so the

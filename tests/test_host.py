@@ -113,6 +113,6 @@ def test_amg_default_options():
     assert (o.tolerance, o.smooth_step, o.max_coarse) == (1e-12, 3, 50)
     assert (o.min_density, o.alpha) == (0.382, 0.25)
     assert o.precision == 0 and o.symmetric == 1
-    assert (o.dense_tail, o.max_colors, o.coarse_colors) == (2048, 32, 4)
+    assert (o.dense_tail, o.max_colors, o.coarse_colors) == (4096, 32, 4)
     assert o.interp_bf16 == 0 and o.fused_vcycle == 0
     assert o.wait_limit_s == 2.0 and o.inject_barrier_stall == 0 and o.gpu_coarsen == 1
