@@ -324,12 +324,20 @@ void galerkin_product(const afp_context* ctx, int64_t n_c, int64_t n_f, const in
   int acc_cap = std::max(1024, (rmax + 31) / 32 * 32);
   // the column -> slot table: rows long enough for the binary search to
   // matter (a hundred entries and more) on levels small enough for a table
-  // of n_c 16-bit slots per warp
+  // of n_c 16-bit slots per warp, as long as the table costs no warps per
+  // block or the rows are long enough (a thousand entries) that one lookup
+  // instead of a deep search is worth fewer warps
+  auto warps_for = [&](size_t extra) {
+    int w = 4;
+    while (w > 1 && (size_t)w * (acc_cap * per_entry + extra) > NUM_SMEM_MAX) --w;
+    return w;
+  };
   const size_t map_bytes = (size_t)n_c * sizeof(unsigned short);
-  const bool map = rmax >= 128 && rmax < 65535 && map_bytes <= 64 * 1024;
-  const size_t per_warp_extra = map ? (map_bytes + 15) / 16 * 16 : 0;
-  int wpn = 4;
-  while (wpn > 1 && (size_t)wpn * (acc_cap * per_entry + per_warp_extra) > NUM_SMEM_MAX) --wpn;
+  const size_t map_extra = (map_bytes + 15) / 16 * 16;
+  const bool map = rmax >= 128 && rmax < 65535 && map_bytes <= 64 * 1024 &&
+                   (warps_for(map_extra) == warps_for(0) || rmax >= 1024);
+  const size_t per_warp_extra = map ? map_extra : 0;
+  const int wpn = warps_for(per_warp_extra);
   if ((size_t)acc_cap * per_entry + per_warp_extra > NUM_SMEM_MAX)  // longest rows accumulate in global memory
     acc_cap = (int)((NUM_SMEM_MAX - per_warp_extra) / per_entry) / 32 * 32;
   const size_t smem_n = (size_t)wpn * (acc_cap * per_entry + per_warp_extra);
