@@ -20,7 +20,7 @@
 // reference's build() would have produced.  Any other scalar operator of
 // these two instantiations (a user getElementMatrix, another template such as
 // the discontinuous P1 triangle, which also has 3 DOFs) is refused with a
-// message and abort(): there is no CPU path for them in this build.  GPU
+// message and abort(): this replacement has no CPU path for them.  GPU
 // failures abort too (the reference's own failures assert or abort).
 //
 // The file also provides the explicit instantiations that the replaced file
@@ -187,7 +187,7 @@ bool gpu_build(BilinearOperator<D, double, double, D, D, D>& op) {
 
 }  // namespace
 
-// An operator the GPU path does not cover: refused (no CPU path in this build).
+// An operator the GPU path does not cover: refused (this replacement has no CPU path).
 [[noreturn]] static void refuse(const char* type) {
   std::cerr << "afepack_gb300: BilinearOperator::build() of " << type
             << " is not on the GPU path (StiffMatrix / MassMatrix on AFEPack's Lagrange P1/P2 triangle or "
