@@ -385,7 +385,7 @@ int gpu_project(const afp_context* ctx, int64_t m64, const int* rp, const int* c
   k_cf_flags<<<grid_for(m, 256), 256, 0, s>>>(m, st1.get(), s2.get(), is_c.get());
   const int nc = (int)exclusive_scan(ctx, is_c.get(), core_at.get(), m);
   out.cf.alloc(ctx, m);
-  k_cf_flags<<<grid_for(m, 256), 256, 0, s>>>(m, st1.get(), s2.get(), out.cf.get());
+  AFP_CUDA(cudaMemcpyAsync(out.cf.get(), is_c.get(), sizeof(int) * m, cudaMemcpyDeviceToDevice, s));
   DevBuf<int> core_point(ctx, nc > 0 ? nc : 1);
   k_cf_core_points<<<grid_for(m, 256), 256, 0, s>>>(m, is_c.get(), core_at.get(), core_point.get());
 
