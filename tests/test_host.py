@@ -105,6 +105,19 @@ def test_errors_without_gpu_are_reported(native):
     assert st in (1, 3)
 
 
+def test_null_arguments_are_invalid_without_a_gpu(native):
+    """Entry points check their arguments before touching a device: NULL
+    handles and pointers are AFP_ERR_INVALID (1), on any machine."""
+    import ctypes as C
+    out = C.c_void_p()
+    assert native.afp_space_create_numbered(None, 2, 1, 4, None, 2, None, None, C.byref(out)) == 1
+    assert native.afp_space_info(None, None, None) == 1
+    assert native.afp_space_download_dofs(None, None, None, None) == 1
+    assert native.afp_quadrature_points(None, 4, None, None) == 1
+    assert native.afp_l2_discretize(None, 4, 0, None, 0, None) == 1
+    assert native.afp_batch_server_submit(None, None, None) == 1
+
+
 def test_amg_default_options():
     """Defaults of afp_amg_opts as set by afp_amg_default_opts (host only):
     the reference's AMGSolver parameters plus the GB300-side choices."""
