@@ -67,7 +67,7 @@ class Request(C.Structure):
 class RequestResult(C.Structure):
     _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("rel_residual", C.c_double),
                 ("queue_seconds", C.c_double), ("setup_seconds", C.c_double), ("latency_seconds", C.c_double),
-                ("device_seconds", C.c_double), ("estimate_bytes", C.c_int64)]
+                ("device_seconds", C.c_double), ("estimate_bytes", C.c_int64), ("measured_bytes", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

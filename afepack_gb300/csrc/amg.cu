@@ -497,12 +497,31 @@ void setup(afp_amg* h, afp_matrix* A, bool lazy) {
     }
     Pattern cpat;
     DevBuf<double> cvals;
-    // A coarse level small enough to become the dense tail (by rows, or by
-    // density up to kDenseTailMax rows) is formed through the dense product;
-    // if it then turns out not to be the tail, the reference-order product
-    // is formed after all (the next splitting needs getPMPt's values).
+    // A coarse level that may be the dense tail (by rows, or by density up
+    // to kDenseTailMax rows) is formed through the dense product; if it then
+    // turns out not to be the tail, the reference-order product is formed
+    // after all (the next splitting needs getPMPt's values).  Whether a
+    // level above dense_tail rows can reach the density rule is first
+    // estimated from the symbolic count of an evenly spaced sample of its
+    // rows (with a margin), so that sparse levels never build the
+    // n_f x n_c intermediate.
     bool dense_done = false;
-    if (o.dense_tail > 0 && P.m <= kDenseTailMax) {
+    bool try_dense = o.dense_tail > 0 && P.m <= kDenseTailMax;
+    if (try_dense && P.m > (int64_t)o.dense_tail) {
+      const int64_t ns = std::min<int64_t>(P.m, 256);
+      std::vector<int> srp(ns + 1, 0), sci;
+      for (int64_t t = 0; t < ns; ++t) {
+        const int64_t i = t * P.m / ns;
+        sci.insert(sci.end(), P.cols.begin() + P.rowptr[i], P.cols.begin() + P.rowptr[i + 1]);
+        srp[t + 1] = (int)sci.size();
+      }
+      DevBuf<int> drp(ctx, ns + 1), dci(ctx, sci.size());
+      drp.upload(srp.data(), ns + 1);
+      dci.upload(sci.data(), sci.size());
+      const int64_t nnz_s = galerkin_nnz(ctx, ns, P.m, drp.get(), dci.get(), arp, aci, dT.rp.get(), dT.ci.get());
+      try_dense = (double)nnz_s / ((double)ns * (double)P.m) >= 0.5 * kDenseTailDensity;
+    }
+    if (try_dense) {
       galerkin_product_dense(ctx, P.m, P.n, dP.rp.get(), dP.ci.get(), dP.va.get(), arp, aci, ava, dT.rp.get(),
                              dT.ci.get(), dT.va.get(), cpat, cvals);
       const double density = (double)cpat.nnz / ((double)P.m * (double)P.m);

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <memory>
 #include <stdexcept>
@@ -77,12 +78,23 @@ struct afp_context {
   // never share them
   double* d_partials = nullptr;
   unsigned* d_retire = nullptr;
+  // device bytes held through DevBuf on this context and their high-water
+  // mark (the server measures each request's footprint with them)
+  mutable std::atomic<int64_t> dev_bytes{0}, dev_peak{0};
 };
 
 namespace afp {
 
 // Makes the context's device current for the calling thread.
 void bind(const afp_context* ctx);
+
+// Adds d bytes to the context's DevBuf total and raises its high-water mark.
+inline void note_device_bytes(const afp_context* ctx, int64_t d) {
+  const int64_t v = ctx->dev_bytes.fetch_add(d, std::memory_order_relaxed) + d;
+  int64_t p = ctx->dev_peak.load(std::memory_order_relaxed);
+  while (v > p && !ctx->dev_peak.compare_exchange_weak(p, v, std::memory_order_relaxed)) {
+  }
+}
 
 // -------------------------------------------------------------- device buffer
 // Stream-ordered device allocation (cudaMallocAsync on the context stream).
@@ -111,9 +123,13 @@ class DevBuf {
     void* p = nullptr;
     AFP_CUDA(cudaMallocAsync(&p, n * sizeof(T), ctx->stream));
     p_ = static_cast<T*>(p);
+    note_device_bytes(ctx, (int64_t)(n * sizeof(T)));
   }
   void release() noexcept {
-    if (p_ != nullptr && ctx_ != nullptr) cudaFreeAsync(p_, ctx_->stream);
+    if (p_ != nullptr && ctx_ != nullptr) {
+      cudaFreeAsync(p_, ctx_->stream);
+      note_device_bytes(ctx_, -(int64_t)(n_ * sizeof(T)));
+    }
     p_ = nullptr;
     n_ = 0;
   }

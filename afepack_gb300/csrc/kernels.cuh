@@ -17,6 +17,12 @@ void galerkin_product(const afp_context* ctx, int64_t n_c, int64_t n_f, const in
                       const int* pt_rowptr, const int* pt_cols, const double* pt_vals, Pattern& out_pat,
                       DevBuf<double>& out_vals);
 
+// Stored entries of the n_rows rows of P A P^T that the given rows of P
+// produce (its symbolic count alone; n_c = columns of the product), to
+// decide how to form a level before forming it.
+int64_t galerkin_nnz(const afp_context* ctx, int64_t n_rows, int64_t n_c, const int* p_rowptr, const int* p_cols,
+                     const int* a_rowptr, const int* a_cols, const int* pt_rowptr, const int* pt_cols);
+
 // Reserves afp_matrix_vmult_noalloc's static staging array on `device` (the
 // current device); called once per context creation (noalloc.cu).
 void noalloc_reserve(int device);

@@ -259,44 +259,79 @@ __global__ void k_rap_numeric(int64_t n_c, const int* __restrict__ prp, const in
   }
 }
 
-}  // namespace
+// The symbolic count of the product: row_len[i] = the unique columns of
+// coarse row i, found by warps, or by blocks for rows that outgrow a warp's
+// table (listed in big, flagged in big_flag).
+struct SymbolicCount {
+  DevBuf<int> row_len, big;
+  DevBuf<unsigned char> big_flag;
+  int hbig = 0, bcap = 1;
+  size_t smem_w = 0, smem_b = 0;
+  unsigned grid = 1;
+};
+constexpr int SYM_WPB = 4;
 
-void galerkin_product(const afp_context* ctx, int64_t n_c, int64_t n_f, const int* prp, const int* pc,
-                      const double* pv, const int* arp, const int* ac, const double* av, const int* trp,
-                      const int* tc, const double* tv, Pattern& out, DevBuf<double>& vals) {
-  (void)n_f;
-  const int wpb = 4;
-  const size_t smem_w = (size_t)wpb * 2 * WARP_CAP * sizeof(int);
-  AFP_CUDA(cudaFuncSetAttribute(k_rap_symbolic_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_w));
-  const unsigned grid = (unsigned)std::min<int64_t>((n_c + wpb - 1) / wpb, (int64_t)ctx->sm_count * 16);
-  DevBuf<int> row_len(ctx, n_c);
-  k_rap_symbolic_warp<<<grid, wpb * 32, smem_w, ctx->stream>>>(n_c, prp, pc, arp, ac, trp, tc, row_len.get(), nullptr,
-                                                               nullptr, nullptr);
+// n_c rows of P; n_cols = columns of the product (sizes the block-level table)
+void symbolic_count(const afp_context* ctx, int64_t n_c, int64_t n_cols, const int* prp, const int* pc,
+                    const int* arp, const int* ac, const int* trp, const int* tc, SymbolicCount& sc) {
+  sc.smem_w = (size_t)SYM_WPB * 2 * WARP_CAP * sizeof(int);
+  AFP_CUDA(cudaFuncSetAttribute(k_rap_symbolic_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc.smem_w));
+  sc.grid = (unsigned)std::min<int64_t>((n_c + SYM_WPB - 1) / SYM_WPB, (int64_t)ctx->sm_count * 16);
+  sc.row_len.alloc(ctx, n_c);
+  k_rap_symbolic_warp<<<sc.grid, SYM_WPB * 32, sc.smem_w, ctx->stream>>>(n_c, prp, pc, arp, ac, trp, tc,
+                                                                         sc.row_len.get(), nullptr, nullptr, nullptr);
   check_launch(ctx, "rap symbolic count");
   // rows whose column set does not fit the warp table go to the block pass
-  DevBuf<int> big(ctx, n_c), nbig(ctx, 1), overflow(ctx, 1);
-  DevBuf<unsigned char> big_flag(ctx, n_c);
+  DevBuf<int> nbig(ctx, 1), overflow(ctx, 1);
+  sc.big.alloc(ctx, n_c);
+  sc.big_flag.alloc(ctx, n_c);
   nbig.zero();
   overflow.zero();
-  k_collect_big<<<grid_for(n_c, 256), 256, 0, ctx->stream>>>(row_len.get(), n_c, big.get(), nbig.get(),
-                                                             big_flag.get());
+  k_collect_big<<<grid_for(n_c, 256), 256, 0, ctx->stream>>>(sc.row_len.get(), n_c, sc.big.get(), nbig.get(),
+                                                             sc.big_flag.get());
   check_launch(ctx, "rap big rows");
-  int hbig = 0;
-  nbig.download(&hbig, 1);
+  nbig.download(&sc.hbig, 1);
   sync(ctx);
-  int bcap = 1;
-  while (bcap < 2 * n_c && bcap < BLOCK_CAP) bcap <<= 1;
-  const size_t smem_b = (size_t)2 * bcap * sizeof(int);
-  if (hbig > 0) {
-    AFP_CUDA(cudaFuncSetAttribute(k_rap_symbolic_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
-    k_rap_symbolic_block<<<(unsigned)std::min(hbig, ctx->sm_count * 2), 256, smem_b, ctx->stream>>>(
-        big.get(), hbig, bcap, prp, pc, arp, ac, trp, tc, row_len.get(), nullptr, nullptr, overflow.get());
+  while (sc.bcap < 2 * n_cols && sc.bcap < BLOCK_CAP) sc.bcap <<= 1;
+  sc.smem_b = (size_t)2 * sc.bcap * sizeof(int);
+  if (sc.hbig > 0) {
+    AFP_CUDA(cudaFuncSetAttribute(k_rap_symbolic_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc.smem_b));
+    k_rap_symbolic_block<<<(unsigned)std::min(sc.hbig, ctx->sm_count * 2), 256, sc.smem_b, ctx->stream>>>(
+        sc.big.get(), sc.hbig, sc.bcap, prp, pc, arp, ac, trp, tc, sc.row_len.get(), nullptr, nullptr,
+        overflow.get());
     check_launch(ctx, "rap symbolic count (block)");
     int hov = 0;
     overflow.download(&hov, 1);
     sync(ctx);
     AFP_REQUIRE(!hov, AFP_ERR_UNSUPPORTED, "Galerkin product row longer than the block-level table");
   }
+}
+
+}  // namespace
+
+int64_t galerkin_nnz(const afp_context* ctx, int64_t n_rows, int64_t n_c, const int* prp, const int* pc,
+                     const int* arp, const int* ac, const int* trp, const int* tc) {
+  SymbolicCount sc;
+  symbolic_count(ctx, n_rows, n_c, prp, pc, arp, ac, trp, tc, sc);
+  DevBuf<int> rowptr(ctx, n_rows + 1);
+  return exclusive_scan(ctx, sc.row_len.get(), rowptr.get(), n_rows);
+}
+
+void galerkin_product(const afp_context* ctx, int64_t n_c, int64_t n_f, const int* prp, const int* pc,
+                      const double* pv, const int* arp, const int* ac, const double* av, const int* trp,
+                      const int* tc, const double* tv, Pattern& out, DevBuf<double>& vals) {
+  (void)n_f;
+  SymbolicCount sc;
+  symbolic_count(ctx, n_c, n_c, prp, pc, arp, ac, trp, tc, sc);
+  const int hbig = sc.hbig, bcap = sc.bcap;
+  const size_t smem_w = sc.smem_w, smem_b = sc.smem_b;
+  const unsigned grid = sc.grid;
+  const int wpb = SYM_WPB;
+  DevBuf<int>& row_len = sc.row_len;
+  DevBuf<int>& big = sc.big;
+  DevBuf<unsigned char>& big_flag = sc.big_flag;
+  DevBuf<int> overflow(ctx, 1);
+  overflow.zero();
   out.m = out.n = n_c;
   out.rowptr.alloc(ctx, n_c + 1);
   out.nnz = exclusive_scan(ctx, row_len.get(), out.rowptr.get(), n_c);

@@ -2,8 +2,9 @@
 //
 // Requests (a mesh/DOF map, per-cell coefficient, nodal data, Dirichlet
 // flags) enter a FIFO queue.  A request is admitted when an execution slot is
-// free and its estimated device footprint fits the HBM budget; the footprint
-// is re-measured after setup and the budget corrected.  Each slot is a host
+// free and its estimated device footprint fits the HBM budget; once its
+// setup is done, the request's measured peak (its allocations on the slot's
+// context) replaces the estimate in the budget.  Each slot is a host
 // thread with its own afp_context, hence its own CUDA stream, so the GPU work
 // of all admitted requests overlaps on the device while their host work (the
 // C/F splitting of AMG setup) runs in parallel on the host cores.  Requests
@@ -39,6 +40,8 @@ struct Job {
   std::vector<int32_t> cells, elem_dof, dirichlet;
   std::vector<double> x;
   int64_t estimate = 0;
+  int64_t charged = 0;     // bytes held against the budget: the estimate, then the measured setup peak
+  int64_t base_bytes = 0;  // the worker context's DevBuf bytes before the request
   Clock::time_point t_submit, t_admit, t_setup, t_done;
   afp_request_result result{};
   bool done = false;
@@ -80,7 +83,10 @@ int64_t estimate_bytes(const Job& j) {
   return b + (64 << 20);
 }
 
-afp_status run(afp_context* ctx, Job& j, const afp_server_opts& o) {
+// the request's peak device bytes so far (its allocations on the worker's context)
+int64_t request_peak(const afp_context* ctx, const Job& j) { return ctx->dev_peak.load() - j.base_bytes; }
+
+afp_status run(afp_server* s, afp_context* ctx, Job& j, const afp_server_opts& o) {
   afp_space* sp = nullptr;
   afp_matrix *K = nullptr, *M = nullptr;
   afp_amg* amg = nullptr;
@@ -115,6 +121,16 @@ afp_status run(afp_context* ctx, Job& j, const afp_server_opts& o) {
   if (o.dense_tail >= 0) mo.dense_tail = o.dense_tail;
   AFP_TRY(afp_amg_setup(K, &mo, &amg));
   j.t_setup = Clock::now();
+  {
+    // the footprint is known now (the CG adds only its vectors): charge the
+    // measured peak instead of the estimate, and let waiting requests in if
+    // that freed budget
+    const int64_t measured = request_peak(ctx, j);
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->in_use += measured - j.charged;
+    j.charged = measured;
+    s->cv_work.notify_all();
+  }
   j.x.assign(j.n_dof, 0.0);
   afp_solve_info info{};
   st = afp_pcg_solve(amg, j.x.data(), b.data(), o.tol, o.maxit, &info);
@@ -146,13 +162,17 @@ void worker_main(afp_server* s) {
       j = s->queue.front();
       s->queue.pop_front();
       s->in_use += j->estimate;
+      j->charged = j->estimate;
       j->t_admit = Clock::now();
     }
-    afp_status st = run(ctx, *j, s->opts);
+    j->base_bytes = ctx->dev_bytes.load();
+    ctx->dev_peak.store(j->base_bytes);
+    afp_status st = run(s, ctx, *j, s->opts);
     {
       std::lock_guard<std::mutex> lk(s->mu);
       j->t_done = Clock::now();
-      s->in_use -= j->estimate;
+      s->in_use -= j->charged;
+      j->result.measured_bytes = request_peak(ctx, *j);
       j->result.status = st;
       j->result.queue_seconds = secs(j->t_submit, j->t_admit);
       j->result.setup_seconds = st == AFP_OK ? secs(j->t_admit, j->t_setup) : 0.0;

@@ -356,7 +356,11 @@ typedef struct afp_request_result {
   double setup_seconds;        /* admission -> hierarchy ready                  */
   double latency_seconds;      /* submit -> solution ready                      */
   double device_seconds;       /* device time of the CG                         */
-  int64_t estimate_bytes;      /* admitted footprint                            */
+  int64_t estimate_bytes;      /* footprint charged at admission (estimate)     */
+  int64_t measured_bytes;      /* peak device bytes the request held; the
+                                  server charges this instead of the estimate
+                                  once the request's setup is done (0 for the
+                                  batch server)                                 */
 } afp_request_result;
 
 typedef struct afp_server_stats {

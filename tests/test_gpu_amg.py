@@ -396,6 +396,28 @@ def test_server_admission_by_memory(ctx):
     assert all(r["status"] == 0 for _, r in out)
 
 
+def test_server_measures_request_footprints(ctx):
+    """Each request's peak device bytes are measured on its slot's context and
+    replace the admission estimate once its setup is done: larger meshes hold
+    more, the budget in use returns to zero when all are done, and the
+    estimate is reported beside the measurement."""
+    from afepack_gb300 import workloads as W
+    from afepack_gb300.serve import Server
+    reqs = [W.request_workload(W.Request(i, n, i % 2 == 1, 9100 + i)) for i, n in enumerate((32, 96, 192))]
+    with Server(workers=2) as srv:
+        out = [srv.wait(t) for t in [srv.submit(wl) for wl in reqs]]
+        st = srv.stats()
+    assert all(r["status"] == 0 for _, r in out)
+    measured = [r["measured_bytes"] for _, r in out]
+    assert 0 < measured[0] < measured[1] < measured[2]
+    assert all(r["estimate_bytes"] > 0 for _, r in out)
+    assert st["in_use_bytes"] == 0
+    # device bytes the mesh arrays alone must occupy: coordinates, cells, DOF map
+    for (_, r), wl in zip(out, reqs):
+        m = wl.mesh
+        assert r["measured_bytes"] >= m.n_vertex * 2 * 8 + m.n_cell * 3 * 4 * 2
+
+
 def test_batch_server_results_same_alone_and_in_the_mix(ctx):
     """Continuous batching against one resident hierarchy: requests submitted
     while others are in flight join free columns between CG iterations; each
