@@ -62,3 +62,23 @@ def test_checker_catches_a_stray_name():
     for child in top.get_children():
         bad += _undefined(child, _module_names(top))
     assert [b[2] for b in bad] == ["lat"]
+
+
+def test_profiled_traffic_ratio_is_read_from_the_committed_summary():
+    """bench.py's roofline `traffic` comes from the committed ncu summary of
+    the batched sweep; a missing or unreadable line would silently report null."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    ratio = bench.profiled_ratio("poisson3d_p1_64", "rows_m_gs_batched")
+    assert ratio is not None and 1.0 <= ratio <= 4.0
+
+
+@pytest.mark.parametrize("name", sorted(f for f in os.listdir(os.path.join(ROOT, "profiles")) if f.endswith(".md")))
+def test_profile_summaries_give_their_command(name):
+    """Every ncu summary names the ncu command that made it, with
+    --clock-control none, and runs committed files only."""
+    text = open(os.path.join(ROOT, "profiles", name)).read()
+    assert "ncu " in text and "--clock-control none" in text, name
+    assert "_work/" not in text and "gpurun" not in text, name
