@@ -7,7 +7,7 @@
 // context) replaces the estimate in the budget.  Each slot is a host
 // thread with its own afp_context, hence its own CUDA stream, so the GPU work
 // of all admitted requests overlaps on the device while their host work (the
-// C/F splitting of AMG setup) runs in parallel on the host cores.  Requests
+// colouring of the AMG setup) runs in parallel on the host cores.  Requests
 // that arrive while others are running are admitted as soon as a slot and
 // memory free up.  All device state of a request -- space, matrices,
 // hierarchy, iterates -- stays resident for its whole life.
